@@ -1,0 +1,173 @@
+/*
+ * nsg.h -- C ABI of libnsg, the GB300 (sm_103a) implementation of NSphere's
+ * per-step shell loop: radial sort -> enclosed mass M(r) and force -> adaptive
+ * leapfrog with adaptive Levi-Civita regularisation.
+ *
+ * The reference (kris-sigurdson/NSphere v0.1.2, src/c/nsphere.c) has no plugin
+ * interface: its step is inline code in main().  Each entry point below names
+ * the reference code it replaces.  Conventions:
+ *   - every call returns NSG_OK (0) or a negative NSG_E* code; the library never
+ *     calls exit() (the reference exits through CLEAN_EXIT, nsphere.c:289-298);
+ *     nsg_last_error() gives the message of the most recent failure;
+ *   - a context owns its device memory and CUDA stream; state stays resident on
+ *     the GPU between steps; one context per host thread;
+ *   - host arrays are plain pointers to contiguous float64 / int32 columns, laid
+ *     out like the reference's particles[component][index] rows
+ *     (nsphere.c:4656-4682): 0 = r, 1 = v_r, 2 = ell, 3 = id (stored as double),
+ *     4 = mu (carried through the sort when the context was created with
+ *     carry_aux = 1);
+ *   - there is no CPU fallback: without a usable sm_103a GPU nsg_create fails.
+ */
+#ifndef NSG_H
+#define NSG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSG_OK 0
+#define NSG_EINVAL (-1)     /* bad argument (null pointer, n out of range, ...) */
+#define NSG_ECUDA (-2)      /* a CUDA runtime call failed */
+#define NSG_ENOMEM (-3)     /* device or pinned-host allocation failed */
+#define NSG_ESTATE (-4)     /* call out of order (e.g. step before upload) */
+#define NSG_EIDS (-5)       /* particle ids are not a permutation of 0..n-1 */
+#define NSG_EDEVICE (-6)    /* a kernel reported an error word (see nsg_status) */
+#define NSG_ETIMEOUT (-7)   /* nsg_sync timed out */
+
+/* Integration method: the reference's internal method_select codes. */
+#define NSG_METHOD_KDK 2          /* fixed-step leapfrog, vel half-step (CLI --method 6), nsphere.c:5484-5559 */
+#define NSG_METHOD_ADAPTIVE 3     /* adaptive leapfrog only (CLI --method 3) */
+#define NSG_METHOD_ADAPTIVE_LC 5  /* adaptive leapfrog + adaptive Levi-Civita (CLI --method 1, default), nsphere.c:5775-5838 */
+
+/* Levi-Civita routing rule for NSG_METHOD_ADAPTIVE_LC. */
+#define NSG_LC_RCRIT 0   /* r < alpha * ell^2 / (G M_i), reference rule nsphere.c:5804-5822 */
+#define NSG_LC_RADIUS 1  /* r < lc_radius */
+#define NSG_LC_OFF 2     /* never */
+
+/* Level scheduling for the adaptive leapfrog. */
+#define NSG_SCHED_PLAIN 0    /* try N = 1, 2, 4, ... as the reference does */
+#define NSG_SCHED_LEARNED 1  /* start each particle at the level its MLP predicts */
+
+/* Device status bits returned by nsg_status (sticky until nsg_clear_status). */
+#define NSG_ST_NAN 0x1u           /* a non-finite radius reached the sort (sorted last) */
+#define NSG_ST_TAU_CAP 0x2u       /* a Levi-Civita step hit max_tau_steps */
+#define NSG_ST_NOT_CONVERGED 0x4u /* a particle used its last level without converging */
+#define NSG_ST_SORT_FALLBACK 0x8u /* the near-sorted bucket sort overflowed; the full radix sort ran */
+#define NSG_ST_QUEUE 0x10u        /* a work queue overflowed (internal error) */
+
+typedef struct nsg_params {
+    double G;              /* effective gravitational constant: VEL_CONV_SQ*G_CONST (nsphere.c:365,373); 1 in G=M=1 units */
+    double M_total;        /* halo mass: HALO_MASS (nsphere.c:371) */
+    double dt;             /* step length */
+    double tol_r;          /* relative radius tolerance, 1e-7 (nsphere.c:5778) */
+    double tol_v;          /* relative velocity tolerance, 1e-7 (nsphere.c:5777) */
+    int64_t max_subdiv;    /* largest subdivision N tried; reference 4096*4096*16 (nsphere.c:5779) */
+    int32_t out_type;      /* 0 coarse, 1 fine, 2 Richardson 4F-3C (nsphere.c:5780) */
+    int32_t N_taumin;      /* tau-steps target of the Levi-Civita guess, 10 (nsphere.c:5781) */
+    int32_t method;        /* NSG_METHOD_* */
+    int32_t lc_rule;       /* NSG_LC_* */
+    double lc_alpha;       /* 0.05 (nsphere.c:5782) */
+    double lc_radius;      /* radius for NSG_LC_RADIUS */
+    int64_t max_tau_steps; /* Levi-Civita tau-step cap, 1e8 (nsphere.c:2273) */
+    int32_t sched;         /* NSG_SCHED_* */
+    int32_t carry_aux;     /* 1: permute a fifth float64 column (mu) with the state */
+    int32_t sort_mode;     /* 0 auto (near-sorted bucket sort, radix fallback), 1 always radix */
+    int32_t reserved0;
+    double point_mass;     /* central point mass added to M_i at the step start (0 = reference) */
+    double point_mass_rate;/* d(point_mass)/dt, applied per step (linear ramp) */
+} nsg_params;
+
+typedef struct nsg_ctx nsg_ctx;
+
+/* Per-kernel timing accumulated while profiling is on (CUDA events on the
+ * context's stream). */
+typedef struct nsg_kernel_stat {
+    char name[32];
+    int64_t launches;
+    double total_ms;
+    double bytes;          /* algorithmic bytes moved by those launches */
+} nsg_kernel_stat;
+
+/* Fills the reference's method-5 defaults in G=M=1 units (dt 5e-4, tol 1e-7,
+ * max_subdiv 2^28, out_type 2, N_taumin 10, r_crit rule with alpha 0.05). */
+int nsg_params_default(nsg_params *p);
+
+/* Creates a context on the current CUDA device.  stream may be NULL (the
+ * context creates its own) or a cudaStream_t the caller owns. */
+int nsg_create(nsg_ctx **ctx, const nsg_params *p, void *stream);
+void nsg_destroy(nsg_ctx *ctx);
+const char *nsg_last_error(nsg_ctx *ctx);   /* ctx may be NULL: last global error */
+int nsg_set_params(nsg_ctx *ctx, const nsg_params *p);
+int nsg_get_params(nsg_ctx *ctx, nsg_params *p);
+
+/* Uploads the state from host columns (the reference's particles[0..3][0..n-1];
+ * aux = particles[4], may be NULL).  ids must be a permutation of 0..n-1, as the
+ * reference's inverse_map requires (nsphere.c:5789-5794).  Replaces nothing in the
+ * reference (its state is host-resident); the upload is the one H2D copy. */
+int nsg_upload(nsg_ctx *ctx, const double *r, const double *vr, const double *ell,
+               const double *id_as_double, const double *aux, int64_t n);
+/* Same with the reference's double ** row table: particles[0..4]. */
+int nsg_upload_particles(nsg_ctx *ctx, double *const *particles, int64_t n);
+/* Same from device pointers (int32 ids). */
+int nsg_upload_device(nsg_ctx *ctx, const double *d_r, const double *d_vr,
+                      const double *d_ell, const int32_t *d_id, const double *d_aux,
+                      int64_t n);
+
+/* Runs nsteps full steps of params.method.  Replaces the body of the time loop at
+ * nsphere.c:5775-5838 (method 5) / :5484-5531 (method 2): sort_particles
+ * (nsphere.c:8662), the inverse_map rebuild, and the per-particle integrators
+ * doAdaptiveFullLeap (nsphere.c:1648) / doAdaptiveFullLeviCivita (nsphere.c:2231). */
+int nsg_step(nsg_ctx *ctx, int nsteps);
+
+/* Sorts the resident state by (r, id) -- sort_particles (nsphere.c:8662) -- and
+ * computes the rank force numerators.  Idempotent. */
+int nsg_sort(nsg_ctx *ctx);
+
+/* Downloads the state in its current array order (after nsg_step: the order of
+ * the sort at the start of the last step, as the reference's particles array). */
+int nsg_download(nsg_ctx *ctx, double *r, double *vr, double *ell,
+                 double *id_as_double, double *aux);
+int nsg_download_particles(nsg_ctx *ctx, double *const *particles);
+/* Device-pointer views of the resident columns (valid until the next call). */
+int nsg_device_state(nsg_ctx *ctx, double **d_r, double **d_vr, double **d_ell,
+                     int32_t **d_id, int64_t *n);
+
+/* Stateless drop-in for sort_particles(double **particles, int npts)
+ * (nsphere.c:8662): uploads the five columns, sorts on the GPU by (r, id),
+ * downloads them permuted.  Uses ctx's buffers and stream. */
+int nsg_sort_particles(nsg_ctx *ctx, double *const *particles, int64_t npts);
+
+/* Looks up k particles by id -- the inverse_map reads of the tracking code
+ * (nsphere.c:5845-5866, 6384-6450).  rank receives the current array index. */
+int nsg_gather(nsg_ctx *ctx, const int32_t *ids, int k, double *r, double *vr,
+               double *ell, int32_t *rank);
+
+/* Total energy of the resident state, K = sum 1/2 m (v_r^2 + ell^2/r^2) and
+ * W = sum m G_num(i)/r_i with the rank enclosed mass of nsphere.c:513.  Sorts the
+ * state first (the sort is a total order, so later steps are unaffected). */
+int nsg_energy(nsg_ctx *ctx, double *K, double *W);
+
+/* Histogram of accepted adaptive-leapfrog levels of the last step: hist[k] for
+ * k < nbins-2; hist[nbins-2] = particles that never converged; hist[nbins-1] =
+ * particles integrated by Levi-Civita. */
+int nsg_level_hist(nsg_ctx *ctx, int64_t *hist, int nbins);
+/* Per-particle accepted level of the last step (int8, -1 = not converged,
+ * 100+k / 99 = Levi-Civita), in current array order. */
+int nsg_levels(nsg_ctx *ctx, int8_t *levels);
+
+int nsg_sync(nsg_ctx *ctx, int timeout_ms);
+int nsg_status(nsg_ctx *ctx, uint32_t *flags);
+int nsg_clear_status(nsg_ctx *ctx);
+
+/* Kernels launched by steps and sorts so far, and steps taken (for reporting). */
+int nsg_counters(nsg_ctx *ctx, int64_t *launches, int64_t *steps);
+
+int nsg_profile(nsg_ctx *ctx, int enable);
+int nsg_profile_read(nsg_ctx *ctx, nsg_kernel_stat *stats, int max, int *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NSG_H */

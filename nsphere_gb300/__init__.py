@@ -1,0 +1,247 @@
+"""nsphere_gb300: GB300-native step loop of NSphere behind the C ABI of include/nsg.h.
+
+This module is a thin ctypes binding of ``libnsg.so`` (built in-tree by
+``nsphere_gb300.build``).  There is no CPU fallback: importing works anywhere, but
+``lib()`` raises when the library is missing and every context creation fails
+without an sm_103a GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libnsg.so")
+
+NSG_OK = 0
+NSG_EINVAL, NSG_ECUDA, NSG_ENOMEM, NSG_ESTATE, NSG_EIDS, NSG_EDEVICE, NSG_ETIMEOUT = (
+    -1, -2, -3, -4, -5, -6, -7)
+METHOD_KDK, METHOD_ADAPTIVE, METHOD_ADAPTIVE_LC = 2, 3, 5
+LC_RCRIT, LC_RADIUS, LC_OFF = 0, 1, 2
+SCHED_PLAIN, SCHED_LEARNED = 0, 1
+ST_NAN, ST_TAU_CAP, ST_NOT_CONVERGED, ST_SORT_FALLBACK, ST_QUEUE = 0x1, 0x2, 0x4, 0x8, 0x10
+
+# exported symbols of include/nsg.h (tests check the library exports each one)
+EXPORTS = [
+    "nsg_params_default", "nsg_create", "nsg_destroy", "nsg_last_error", "nsg_set_params",
+    "nsg_get_params", "nsg_upload", "nsg_upload_particles", "nsg_upload_device", "nsg_step",
+    "nsg_sort", "nsg_download", "nsg_download_particles", "nsg_device_state",
+    "nsg_sort_particles", "nsg_gather", "nsg_energy", "nsg_level_hist", "nsg_levels",
+    "nsg_sync", "nsg_status", "nsg_clear_status", "nsg_profile", "nsg_profile_read", "nsg_counters",
+]
+
+
+class Params(C.Structure):
+    """Mirror of ``nsg_params`` (include/nsg.h)."""
+    _fields_ = [
+        ("G", C.c_double), ("M_total", C.c_double), ("dt", C.c_double),
+        ("tol_r", C.c_double), ("tol_v", C.c_double), ("max_subdiv", C.c_int64),
+        ("out_type", C.c_int32), ("N_taumin", C.c_int32), ("method", C.c_int32),
+        ("lc_rule", C.c_int32), ("lc_alpha", C.c_double), ("lc_radius", C.c_double),
+        ("max_tau_steps", C.c_int64), ("sched", C.c_int32), ("carry_aux", C.c_int32),
+        ("sort_mode", C.c_int32), ("reserved0", C.c_int32), ("point_mass", C.c_double),
+        ("point_mass_rate", C.c_double),
+    ]
+
+
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("total_ms", C.c_double),
+                ("bytes", C.c_double)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libnsg.so; raises if it was not built (no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libnsg.so is not built: run `python -c \"import __graft_entry__ as g; "
+                           "g.build()\"` (needs nvcc); there is no CPU fallback")
+    L = C.CDLL(LIB_PATH)
+    P, I64, I32, D = C.c_void_p, C.c_int64, C.c_int32, C.c_double
+    sig = {
+        "nsg_params_default": [C.POINTER(Params)],
+        "nsg_create": [C.POINTER(P), C.POINTER(Params), P],
+        "nsg_set_params": [P, C.POINTER(Params)],
+        "nsg_get_params": [P, C.POINTER(Params)],
+        "nsg_upload": [P, P, P, P, P, P, I64],
+        "nsg_upload_particles": [P, P, I64],
+        "nsg_upload_device": [P, P, P, P, P, P, I64],
+        "nsg_step": [P, C.c_int],
+        "nsg_sort": [P],
+        "nsg_download": [P, P, P, P, P, P],
+        "nsg_download_particles": [P, P],
+        "nsg_device_state": [P, P, P, P, P, P],
+        "nsg_sort_particles": [P, P, I64],
+        "nsg_gather": [P, P, C.c_int, P, P, P, P],
+        "nsg_energy": [P, C.POINTER(D), C.POINTER(D)],
+        "nsg_level_hist": [P, P, C.c_int],
+        "nsg_levels": [P, P],
+        "nsg_sync": [P, C.c_int],
+        "nsg_status": [P, C.POINTER(C.c_uint32)],
+        "nsg_clear_status": [P],
+        "nsg_profile": [P, C.c_int],
+        "nsg_counters": [P, C.POINTER(I64), C.POINTER(I64)],
+        "nsg_profile_read": [P, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    L.nsg_destroy.argtypes = [P]
+    L.nsg_destroy.restype = None
+    L.nsg_last_error.argtypes = [P]
+    L.nsg_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+class NsgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("nsg error %d: %s" % (code, msg))
+        self.code = code
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().nsg_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError("nsg_params has no field %r" % k)
+        setattr(p, k, v)
+    return p
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Context:
+    """One libnsg context: device-resident state and its stream."""
+
+    def __init__(self, params: Params | None = None, stream: int | None = None):
+        self._L = lib()
+        self.params = params if params is not None else default_params()
+        h = C.c_void_p()
+        rc = self._L.nsg_create(C.byref(h), C.byref(self.params), C.c_void_p(stream) if stream else None)
+        if rc != NSG_OK:
+            raise NsgError(rc, self._L.nsg_last_error(None).decode())
+        self._h = h
+        self.n = 0
+
+    def _check(self, rc):
+        if rc != NSG_OK:
+            raise NsgError(rc, self._L.nsg_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.nsg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_params(self, params: Params):
+        self._check(self._L.nsg_set_params(self._h, C.byref(params)))
+        self.params = params
+
+    def upload(self, r, vr, ell, ids, aux=None):
+        r, vr, ell = (np.ascontiguousarray(x, dtype=np.float64) for x in (r, vr, ell))
+        idd = np.ascontiguousarray(ids, dtype=np.float64)
+        aux = None if aux is None else np.ascontiguousarray(aux, dtype=np.float64)
+        n = r.shape[0]
+        if not (vr.shape[0] == ell.shape[0] == idd.shape[0] == n):
+            raise ValueError("columns must have equal length")
+        self._check(self._L.nsg_upload(self._h, _ptr(r), _ptr(vr), _ptr(ell), _ptr(idd), _ptr(aux), n))
+        self.n = n
+
+    def step(self, nsteps: int = 1):
+        self._check(self._L.nsg_step(self._h, int(nsteps)))
+
+    def sort(self):
+        self._check(self._L.nsg_sort(self._h))
+
+    def download(self, with_aux: bool = False):
+        n = self.n
+        r, vr, ell, idd = (np.empty(n) for _ in range(4))
+        aux = np.empty(n) if with_aux else None
+        self._check(self._L.nsg_download(self._h, _ptr(r), _ptr(vr), _ptr(ell), _ptr(idd), _ptr(aux)))
+        out = (r, vr, ell, idd.astype(np.int32))
+        return out + ((aux,) if with_aux else ())
+
+    def gather(self, ids):
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        k = ids.shape[0]
+        r, vr, ell = np.empty(k), np.empty(k), np.empty(k)
+        rank = np.empty(k, dtype=np.int32)
+        self._check(self._L.nsg_gather(self._h, _ptr(ids), k, _ptr(r), _ptr(vr), _ptr(ell), _ptr(rank)))
+        return r, vr, ell, rank
+
+    def energy(self):
+        K, W = C.c_double(), C.c_double()
+        self._check(self._L.nsg_energy(self._h, C.byref(K), C.byref(W)))
+        return K.value, W.value
+
+    def level_hist(self, nbins: int = 66):
+        h = np.zeros(nbins, dtype=np.int64)
+        self._check(self._L.nsg_level_hist(self._h, _ptr(h), nbins))
+        return h
+
+    def levels(self):
+        lv = np.empty(self.n, dtype=np.int8)
+        self._check(self._L.nsg_levels(self._h, _ptr(lv)))
+        return lv
+
+    def sync(self, timeout_ms: int = -1):
+        self._check(self._L.nsg_sync(self._h, timeout_ms))
+
+    def status(self) -> int:
+        s = C.c_uint32()
+        self._check(self._L.nsg_status(self._h, C.byref(s)))
+        return s.value
+
+    def clear_status(self):
+        self._check(self._L.nsg_clear_status(self._h))
+
+    def counters(self):
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self._L.nsg_counters(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def profile(self, enable: bool = True):
+        self._check(self._L.nsg_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        arr = (KernelStat * 64)()
+        cnt = C.c_int()
+        self._check(self._L.nsg_profile_read(self._h, arr, 64, C.byref(cnt)))
+        return [dict(name=arr[i].name.decode(), launches=arr[i].launches,
+                     total_ms=arr[i].total_ms, bytes=arr[i].bytes) for i in range(min(cnt.value, 64))]
+
+
+def sort_particles(ctx: Context, particles: np.ndarray):
+    """Drop-in for the reference's ``sort_particles(double **particles, int npts)``
+    on a (4 or 5, n) float64 table, sorted in place on the GPU."""
+    if particles.dtype != np.float64 or not particles.flags.c_contiguous:
+        raise ValueError("particles must be a C-contiguous float64 (k, n) array")
+    n = particles.shape[1]
+    rows = (C.c_void_p * 5)(*[particles[min(i, particles.shape[0] - 1)].ctypes.data for i in range(5)])
+    ctx._check(ctx._L.nsg_sort_particles(ctx._h, rows, n))

@@ -1,0 +1,672 @@
+// nsg_api.cu -- the extern "C" entry points of libnsg (declared in include/nsg.h):
+// context lifetime, device buffers, host <-> device transfer, step orchestration,
+// diagnostics and profiling.
+#include <cstdio>
+#include <cstring>
+#include <chrono>
+#include <thread>
+
+#include "nsg_internal.cuh"
+
+namespace nsg {
+
+static thread_local std::string g_last_err;
+
+int set_err(nsg_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    g_last_err = msg;
+    return code;
+}
+
+int cuda_err(nsg_ctx *c, cudaError_t e, const char *what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return set_err(c, e == cudaErrorMemoryAllocation ? NSG_ENOMEM : NSG_ECUDA, m);
+}
+
+int grid_for(nsg_ctx *c, int64_t n, int threads, int per_sm)
+{
+    int64_t want = (n + threads - 1) / threads;
+    int64_t cap = (int64_t)c->num_sms * per_sm;
+    if (want < 1) want = 1;
+    return (int)(want < cap ? want : cap);
+}
+
+ProfScope::ProfScope(nsg_ctx *c_, const char *name_, double bytes_) : c(c_), name(name_), bytes(bytes_)
+{
+    if (!c->profiling) return;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->stream);
+}
+
+ProfScope::~ProfScope()
+{
+    if (!c->profiling || !e0) return;
+    cudaEventRecord(e1, c->stream);
+    c->ev_pool.push_back(e0);
+    c->ev_pool.push_back(e1);
+    // the name and bytes ride along: stats are resolved at flush time
+    KernelStat ks;
+    ks.name = name;
+    ks.bytes = bytes;
+    ks.launches = -1;  // pending marker, resolved by prof_flush
+    c->stats.push_back(ks);
+}
+
+void prof_flush(nsg_ctx *c)
+{
+    // pending entries pair with ev_pool events in order
+    std::vector<KernelStat> merged;
+    size_t ev = 0;
+    cudaStreamSynchronize(c->stream);
+    for (auto &ks : c->stats) {
+        if (ks.launches != -1) { merged.push_back(ks); continue; }
+        float ms = 0.f;
+        if (ev + 1 < c->ev_pool.size()) {
+            cudaEventElapsedTime(&ms, c->ev_pool[ev], c->ev_pool[ev + 1]);
+            cudaEventDestroy(c->ev_pool[ev]);
+            cudaEventDestroy(c->ev_pool[ev + 1]);
+        }
+        ev += 2;
+        bool found = false;
+        for (auto &m : merged)
+            if (m.name == ks.name) { m.launches += 1; m.total_ms += ms; m.bytes += ks.bytes; found = true; break; }
+        if (!found) { KernelStat k2 = ks; k2.launches = 1; k2.total_ms = ms; merged.push_back(k2); }
+    }
+    c->ev_pool.clear();
+    c->stats.swap(merged);
+}
+
+// --------------------------------------------------------- small kernels
+
+__global__ void k_ids_from_double(const double *__restrict__ src, int32_t *__restrict__ dst,
+                                  int64_t n, unsigned int *bad)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        double x = src[k];
+        int32_t v = -1;
+        if (x >= 0.0 && x < (double)n && x == floor(x)) v = (int32_t)x;
+        else atomicOr(bad, 1u);
+        dst[k] = v;
+    }
+}
+
+// Each id must occur exactly once: count into inv (used as scratch), then check.
+__global__ void k_count_ids(const int32_t *__restrict__ id, int64_t n, int32_t *__restrict__ cnt,
+                            unsigned int *bad)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int32_t j = id[k];
+        if (j < 0 || j >= n) { atomicOr(bad, 1u); continue; }
+        atomicAdd(&cnt[j], 1);
+    }
+}
+
+__global__ void k_check_counts(const int32_t *__restrict__ cnt, int64_t n, unsigned int *bad)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        if (cnt[k] != 1) atomicOr(bad, 1u);
+}
+
+__global__ void k_ids_to_double(const int32_t *__restrict__ src, double *__restrict__ dst, int64_t n)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        dst[k] = (double)src[k];
+}
+
+__global__ void k_gather_ids(const int32_t *__restrict__ ids, int k, const int32_t *__restrict__ inv,
+                             const double *__restrict__ r, const double *__restrict__ v,
+                             const double *__restrict__ l, int64_t n, double *__restrict__ out,
+                             int32_t *__restrict__ rank)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= k) return;
+    int32_t j = ids[t];
+    int32_t p = (j >= 0 && j < n) ? inv[j] : -1;
+    rank[t] = p;
+    if (p < 0) { out[3 * t] = out[3 * t + 1] = out[3 * t + 2] = __longlong_as_double(0x7ff8000000000000ll); return; }
+    out[3 * t] = r[p];
+    out[3 * t + 1] = v[p];
+    out[3 * t + 2] = l[p];
+}
+
+__global__ void k_build_inv(const int32_t *__restrict__ id, int64_t n, int32_t *__restrict__ inv)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        inv[id[k]] = (int32_t)k;
+}
+
+__global__ void k_level_hist(const int8_t *__restrict__ lv, int64_t n, unsigned long long *hist)
+{
+    __shared__ unsigned int h[kStatBins];
+    for (int b = threadIdx.x; b < kStatBins; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int x = lv[k];
+        int b;
+        if (x >= 0 && x < kMaxLevels) b = x;
+        else if (x == kLevelNotConverged) b = kMaxLevels;
+        else b = kMaxLevels + 1;  // Levi-Civita
+        atomicAdd(&h[b], 1u);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kStatBins; b += blockDim.x)
+        if (h[b]) atomicAdd(&hist[b], (unsigned long long)h[b]);
+}
+
+__global__ void k_advance_point_mass(DevCounters *ctr, double rate_dt)
+{
+    ctr->point_mass += rate_dt;
+}
+
+}  // namespace nsg
+
+using namespace nsg;
+
+// ------------------------------------------------------------------ memory
+
+static void free_buffers(nsg_ctx *c)
+{
+    auto f = [](auto *&p) { if (p) cudaFree((void *)p); p = nullptr; };
+    for (int b = 0; b < 2; b++) {
+        f(c->r[b]); f(c->vr[b]); f(c->ell[b]); f(c->aux[b]); f(c->id[b]);
+        f(c->keys[b]); f(c->vals[b]); f(c->q_idx[b]); f(c->q_r[b]); f(c->q_v[b]);
+    }
+    f(c->a0); f(c->inv); f(c->level); f(c->tile_counts); f(c->digit_tot); f(c->lc_idx);
+    f(c->red_part); f(c->stage_d);
+    c->cap = 0;
+}
+
+static int ensure_capacity(nsg_ctx *c, int64_t n)
+{
+    if (n <= c->cap) return NSG_OK;
+    free_buffers(c);
+    const size_t d8 = (size_t)n * 8, d4 = (size_t)n * 4;
+    const int64_t ntiles = (n + kRadixTile - 1) / kRadixTile;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](auto *&p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc((void **)&p, bytes ? bytes : 16);
+    };
+    for (int b = 0; b < 2; b++) {
+        A(c->r[b], d8); A(c->vr[b], d8); A(c->ell[b], d8); A(c->id[b], d4);
+        if (c->p.carry_aux) A(c->aux[b], d8);
+        A(c->keys[b], d8); A(c->vals[b], d4);
+        A(c->q_idx[b], d4); A(c->q_r[b], d8); A(c->q_v[b], d8);
+    }
+    A(c->a0, d8); A(c->inv, d4); A(c->level, (size_t)n);
+    A(c->tile_counts, (size_t)ntiles * kRadixBuckets * 4); A(c->digit_tot, kRadixBuckets * 4);
+    A(c->lc_idx, d4); A(c->red_part, 2 * kReduceBlocks * 8); A(c->stage_d, d8);
+    if (e != cudaSuccess) {
+        free_buffers(c);
+        return cuda_err(c, e, "device allocation");
+    }
+    c->cap = n;
+    return NSG_OK;
+}
+
+static int check_ctx(nsg_ctx *c)
+{
+    if (!c) return set_err(nullptr, NSG_EINVAL, "null context");
+    return NSG_OK;
+}
+
+static int check_params(nsg_ctx *c, const nsg_params *p)
+{
+    if (!p) return set_err(c, NSG_EINVAL, "null params");
+    if (!(p->dt > 0.0) || !isfinite(p->dt)) return set_err(c, NSG_EINVAL, "dt must be positive and finite");
+    if (p->method != NSG_METHOD_KDK && p->method != NSG_METHOD_ADAPTIVE && p->method != NSG_METHOD_ADAPTIVE_LC)
+        return set_err(c, NSG_EINVAL, "unknown method");
+    if (p->max_subdiv < 1) return set_err(c, NSG_EINVAL, "max_subdiv must be >= 1");
+    if (p->out_type < 0 || p->out_type > 2) return set_err(c, NSG_EINVAL, "out_type must be 0, 1 or 2");
+    if (p->lc_rule < 0 || p->lc_rule > 2) return set_err(c, NSG_EINVAL, "unknown lc_rule");
+    if (p->max_tau_steps < 0) return set_err(c, NSG_EINVAL, "max_tau_steps must be >= 0");
+    if (p->sched != NSG_SCHED_PLAIN && p->sched != NSG_SCHED_LEARNED) return set_err(c, NSG_EINVAL, "unknown sched");
+    return NSG_OK;
+}
+
+extern "C" {
+
+int nsg_params_default(nsg_params *p)
+{
+    if (!p) return set_err(nullptr, NSG_EINVAL, "null params");
+    memset(p, 0, sizeof(*p));
+    p->G = 1.0;
+    p->M_total = 1.0;
+    p->dt = 5.0e-4;
+    p->tol_r = 1.0e-7;
+    p->tol_v = 1.0e-7;
+    p->max_subdiv = 4096LL * 4096LL * 16LL;
+    p->out_type = 2;
+    p->N_taumin = 10;
+    p->method = NSG_METHOD_ADAPTIVE_LC;
+    p->lc_rule = NSG_LC_RCRIT;
+    p->lc_alpha = 0.05;
+    p->lc_radius = 1.0e-3;
+    p->max_tau_steps = 100000000LL;
+    p->sched = NSG_SCHED_PLAIN;
+    p->carry_aux = 0;
+    p->sort_mode = 0;
+    return NSG_OK;
+}
+
+int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
+{
+    if (!out) return set_err(nullptr, NSG_EINVAL, "null ctx pointer");
+    *out = nullptr;
+    if (int rc = check_params(nullptr, p)) return rc;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_err(nullptr, NSG_ECUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return set_err(nullptr, NSG_ECUDA, std::string("device query: ") + cudaGetErrorString(e));
+    if (prop.major * 10 + prop.minor < 100)
+        return set_err(nullptr, NSG_ECUDA, "libnsg is built for sm_103a (GB300); this device is sm_" +
+                                               std::to_string(prop.major * 10 + prop.minor));
+    nsg_ctx *c = new nsg_ctx();
+    c->p = *p;
+    c->device = dev;
+    c->num_sms = prop.multiProcessorCount;
+    if (stream) c->stream = (cudaStream_t)stream;
+    else {
+        e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        c->own_stream = true;
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->ctr, sizeof(DevCounters));
+    if (e == cudaSuccess) e = cudaMemset(c->ctr, 0, sizeof(DevCounters));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_ctr, sizeof(DevCounters));
+    if (e == cudaSuccess && p->point_mass != 0.0)
+        e = cudaMemcpy(&c->ctr->point_mass, &p->point_mass, sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        int rc = cuda_err(nullptr, e, "context setup");
+        nsg_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return NSG_OK;
+}
+
+void nsg_destroy(nsg_ctx *c)
+{
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
+    for (auto ev : c->ev_pool) cudaEventDestroy(ev);
+    free_buffers(c);
+    if (c->ctr) cudaFree(c->ctr);
+    if (c->h_ctr) cudaFreeHost(c->h_ctr);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char *nsg_last_error(nsg_ctx *c)
+{
+    if (c) return c->err.c_str();
+    return g_last_err.c_str();
+}
+
+int nsg_set_params(nsg_ctx *c, const nsg_params *p)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (int rc = check_params(c, p)) return rc;
+    if (p->carry_aux != c->p.carry_aux && c->n > 0)
+        return set_err(c, NSG_ESTATE, "carry_aux cannot change while a state is resident");
+    bool pm_changed = (p->point_mass != c->p.point_mass);
+    c->p = *p;
+    if (pm_changed) {
+        cudaError_t e = cudaMemcpyAsync(&c->ctr->point_mass, &c->p.point_mass, sizeof(double),
+                                        cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_err(c, e, "point mass update");
+        c->sorted = false;  // a0 depends on the point mass
+    }
+    return NSG_OK;
+}
+
+int nsg_get_params(nsg_ctx *c, nsg_params *p)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (!p) return set_err(c, NSG_EINVAL, "null params");
+    *p = c->p;
+    return NSG_OK;
+}
+
+static int validate_ids(nsg_ctx *c, const int32_t *d_id, int64_t n, unsigned int bad_in)
+{
+    // inv doubles as the count array here
+    cudaError_t e = cudaMemsetAsync(c->inv, 0, (size_t)n * 4, c->stream);
+    unsigned int *d_bad = &c->ctr->pad;
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, 4, c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "id validation setup");
+    k_count_ids<<<grid_for(c, n, 256), 256, 0, c->stream>>>(d_id, n, c->inv, d_bad);
+    k_check_counts<<<grid_for(c, n, 256), 256, 0, c->stream>>>(c->inv, n, d_bad);
+    unsigned int bad = 0;
+    e = cudaMemcpyAsync(&c->h_ctr->pad, d_bad, 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "id validation");
+    bad = c->h_ctr->pad | bad_in;
+    if (bad) return set_err(c, NSG_EIDS, "particle ids must be a permutation of 0..n-1");
+    return NSG_OK;
+}
+
+static int upload_common(nsg_ctx *c, int64_t n)
+{
+    if (n <= 0 || n > (int64_t)0x7fffffff) return set_err(c, NSG_EINVAL, "n must be in [1, 2^31-1]");
+    if (int rc = ensure_capacity(c, n)) return rc;
+    c->n = n;
+    c->cur = 0;
+    c->sorted = false;
+    c->inv_valid = false;
+    return NSG_OK;
+}
+
+int nsg_upload(nsg_ctx *c, const double *r, const double *vr, const double *ell,
+               const double *id_as_double, const double *aux, int64_t n)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (!r || !vr || !ell || !id_as_double) return set_err(c, NSG_EINVAL, "null column");
+    if (c->p.carry_aux && !aux) return set_err(c, NSG_EINVAL, "carry_aux set but aux is null");
+    if (int rc = upload_common(c, n)) return rc;
+    const size_t b = (size_t)n * 8;
+    cudaStream_t s = c->stream;
+    cudaError_t e = cudaMemcpyAsync(c->r[0], r, b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->vr[0], vr, b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->ell[0], ell, b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->stage_d, id_as_double, b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && c->p.carry_aux) e = cudaMemcpyAsync(c->aux[0], aux, b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&c->ctr->pad, 0, 4, s);
+    if (e != cudaSuccess) return cuda_err(c, e, "upload copy");
+    k_ids_from_double<<<grid_for(c, n, 256), 256, 0, s>>>(c->stage_d, c->id[0], n, &c->ctr->pad);
+    return validate_ids(c, c->id[0], n, 0);
+}
+
+int nsg_upload_particles(nsg_ctx *c, double *const *particles, int64_t n)
+{
+    if (!particles) return set_err(c, NSG_EINVAL, "null particles");
+    return nsg_upload(c, particles[0], particles[1], particles[2], particles[3],
+                      c && c->p.carry_aux ? particles[4] : nullptr, n);
+}
+
+int nsg_upload_device(nsg_ctx *c, const double *d_r, const double *d_vr, const double *d_ell,
+                      const int32_t *d_id, const double *d_aux, int64_t n)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (!d_r || !d_vr || !d_ell || !d_id) return set_err(c, NSG_EINVAL, "null column");
+    if (c->p.carry_aux && !d_aux) return set_err(c, NSG_EINVAL, "carry_aux set but aux is null");
+    if (int rc = upload_common(c, n)) return rc;
+    const size_t b = (size_t)n * 8;
+    cudaStream_t s = c->stream;
+    cudaError_t e = cudaMemcpyAsync(c->r[0], d_r, b, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->vr[0], d_vr, b, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->ell[0], d_ell, b, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->id[0], d_id, (size_t)n * 4, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && c->p.carry_aux) e = cudaMemcpyAsync(c->aux[0], d_aux, b, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_err(c, e, "upload copy");
+    return validate_ids(c, c->id[0], n, 0);
+}
+
+int nsg_sort(nsg_ctx *c)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
+    return sort_state(c);
+}
+
+int nsg_step(nsg_ctx *c, int nsteps)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
+    if (nsteps < 0) return set_err(c, NSG_EINVAL, "nsteps must be >= 0");
+    for (int j = 0; j < nsteps; j++) {
+        int rc = NSG_OK;
+        if (c->p.method == NSG_METHOD_KDK) {
+            // the reference sorts once before its time loop (nsphere.c:5339-5342)
+            if (!c->sorted) rc = sort_state(c);
+            if (!rc) rc = kdk_first_half(c);
+            if (!rc) rc = sort_state(c);
+            if (!rc) rc = kdk_second_half(c);
+        } else {
+            rc = sort_state(c);
+            if (!rc) rc = integrate_adaptive(c);
+            c->sorted = false;  // radii moved
+        }
+        if (rc) return rc;
+        if (c->p.point_mass_rate != 0.0) {
+            k_advance_point_mass<<<1, 1, 0, c->stream>>>(c->ctr, c->p.point_mass_rate * c->p.dt);
+            c->launches += 1;
+            c->p.point_mass += c->p.point_mass_rate * c->p.dt;
+            c->sorted = false;
+        }
+        c->steps_done++;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(c, e, "step launch");
+    if (c->profiling) prof_flush(c);
+    return NSG_OK;
+}
+
+int nsg_download(nsg_ctx *c, double *r, double *vr, double *ell, double *id_as_double, double *aux)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
+    const int s = c->cur;
+    const size_t b = (size_t)c->n * 8;
+    cudaStream_t st = c->stream;
+    cudaError_t e = cudaSuccess;
+    if (r) e = cudaMemcpyAsync(r, c->r[s], b, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && vr) e = cudaMemcpyAsync(vr, c->vr[s], b, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && ell) e = cudaMemcpyAsync(ell, c->ell[s], b, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && aux && c->p.carry_aux) e = cudaMemcpyAsync(aux, c->aux[s], b, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && id_as_double) {
+        k_ids_to_double<<<grid_for(c, c->n, 256), 256, 0, st>>>(c->id[s], c->stage_d, c->n);
+        e = cudaMemcpyAsync(id_as_double, c->stage_d, b, cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_err(c, e, "download");
+    return NSG_OK;
+}
+
+int nsg_download_particles(nsg_ctx *c, double *const *particles)
+{
+    if (!particles) return set_err(c, NSG_EINVAL, "null particles");
+    return nsg_download(c, particles[0], particles[1], particles[2], particles[3],
+                        c && c->p.carry_aux ? particles[4] : nullptr);
+}
+
+int nsg_device_state(nsg_ctx *c, double **d_r, double **d_vr, double **d_ell, int32_t **d_id, int64_t *n)
+{
+    if (int rc = check_ctx(c)) return rc;
+    const int s = c->cur;
+    if (d_r) *d_r = c->r[s];
+    if (d_vr) *d_vr = c->vr[s];
+    if (d_ell) *d_ell = c->ell[s];
+    if (d_id) *d_id = c->id[s];
+    if (n) *n = c->n;
+    return NSG_OK;
+}
+
+int nsg_sort_particles(nsg_ctx *c, double *const *particles, int64_t npts)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (int rc = nsg_upload_particles(c, particles, npts)) return rc;
+    if (int rc = sort_state(c)) return rc;
+    return nsg_download_particles(c, particles);
+}
+
+int nsg_gather(nsg_ctx *c, const int32_t *ids, int k, double *r, double *vr, double *ell, int32_t *rank)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
+    if (k < 0 || (k > 0 && !ids)) return set_err(c, NSG_EINVAL, "bad id list");
+    if (k == 0) return NSG_OK;
+    if (!c->inv_valid) {
+        // no sort since the upload: map the ids of the uploaded order
+        k_build_inv<<<grid_for(c, c->n, 256), 256, 0, c->stream>>>(c->id[c->cur], c->n, c->inv);
+        c->inv_valid = true;
+    }
+    int32_t *d_ids = nullptr, *d_rank = nullptr;
+    double *d_out = nullptr;
+    cudaError_t e = cudaMallocAsync((void **)&d_ids, (size_t)k * 4, c->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&d_rank, (size_t)k * 4, c->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&d_out, (size_t)k * 24, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_ids, ids, (size_t)k * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "gather setup");
+    const int s = c->cur;
+    k_gather_ids<<<(k + 127) / 128, 128, 0, c->stream>>>(d_ids, k, c->inv, c->r[s], c->vr[s], c->ell[s],
+                                                         c->n, d_out, d_rank);
+    std::vector<double> h((size_t)k * 3);
+    std::vector<int32_t> hr((size_t)k);
+    e = cudaMemcpyAsync(h.data(), d_out, (size_t)k * 24, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hr.data(), d_rank, (size_t)k * 4, cudaMemcpyDeviceToHost, c->stream);
+    cudaFreeAsync(d_ids, c->stream);
+    cudaFreeAsync(d_rank, c->stream);
+    cudaFreeAsync(d_out, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "gather");
+    for (int t = 0; t < k; t++) {
+        if (r) r[t] = h[3 * t];
+        if (vr) vr[t] = h[3 * t + 1];
+        if (ell) ell[t] = h[3 * t + 2];
+        if (rank) rank[t] = hr[t];
+    }
+    return NSG_OK;
+}
+
+int nsg_energy(nsg_ctx *c, double *K, double *W)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
+    if (!c->sorted)
+        if (int rc = sort_state(c)) return rc;
+    cudaError_t e = cudaMemcpyAsync(c->h_ctr->energy, c->ctr->energy, 16, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "energy readback");
+    if (K) *K = c->h_ctr->energy[0];
+    if (W) *W = c->h_ctr->energy[1];
+    return NSG_OK;
+}
+
+int nsg_level_hist(nsg_ctx *c, int64_t *hist, int nbins)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (!hist || nbins < 3) return set_err(c, NSG_EINVAL, "hist needs at least 3 bins");
+    if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
+    cudaError_t e = cudaMemsetAsync(c->ctr->level_hist, 0, sizeof(c->ctr->level_hist), c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "hist reset");
+    k_level_hist<<<grid_for(c, c->n, 256, 4), 256, 0, c->stream>>>(c->level, c->n, c->ctr->level_hist);
+    e = cudaMemcpyAsync(c->h_ctr->level_hist, c->ctr->level_hist, sizeof(c->ctr->level_hist),
+                        cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "hist readback");
+    for (int b = 0; b < nbins; b++) hist[b] = 0;
+    for (int k = 0; k < kMaxLevels; k++) {
+        int b = k < nbins - 2 ? k : nbins - 3;
+        hist[b] += (int64_t)c->h_ctr->level_hist[k];
+    }
+    hist[nbins - 2] = (int64_t)c->h_ctr->level_hist[kMaxLevels];
+    hist[nbins - 1] = (int64_t)c->h_ctr->level_hist[kMaxLevels + 1];
+    return NSG_OK;
+}
+
+int nsg_levels(nsg_ctx *c, int8_t *levels)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (!levels) return set_err(c, NSG_EINVAL, "null levels");
+    cudaError_t e = cudaMemcpyAsync(levels, c->level, (size_t)c->n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "levels readback");
+    return NSG_OK;
+}
+
+int nsg_sync(nsg_ctx *c, int timeout_ms)
+{
+    if (int rc = check_ctx(c)) return rc;
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(c->stream);
+        if (e == cudaSuccess) e = cudaStreamQuery(c->side);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return cuda_err(c, e, "sync");
+        if (timeout_ms >= 0 &&
+            std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeout_ms))
+            return set_err(c, NSG_ETIMEOUT, "nsg_sync timed out");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    uint32_t st = 0;
+    nsg_status(c, &st);
+    if (st & (NSG_ST_TAU_CAP | NSG_ST_QUEUE))
+        return set_err(c, NSG_EDEVICE, "device status word 0x" + std::to_string(st));
+    return NSG_OK;
+}
+
+int nsg_status(nsg_ctx *c, uint32_t *flags)
+{
+    if (int rc = check_ctx(c)) return rc;
+    cudaError_t e = cudaMemcpyAsync(&c->h_ctr->status, &c->ctr->status, 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "status readback");
+    if (flags) *flags = c->h_ctr->status;
+    return NSG_OK;
+}
+
+int nsg_clear_status(nsg_ctx *c)
+{
+    if (int rc = check_ctx(c)) return rc;
+    cudaError_t e = cudaMemsetAsync(&c->ctr->status, 0, 4, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "status clear");
+    return NSG_OK;
+}
+
+int nsg_counters(nsg_ctx *c, int64_t *launches, int64_t *steps)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (launches) *launches = c->launches;
+    if (steps) *steps = c->steps_done;
+    return NSG_OK;
+}
+
+int nsg_profile(nsg_ctx *c, int enable)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (c->profiling) prof_flush(c);
+    c->profiling = enable != 0;
+    c->stats.clear();
+    return NSG_OK;
+}
+
+int nsg_profile_read(nsg_ctx *c, nsg_kernel_stat *stats, int max, int *count)
+{
+    if (int rc = check_ctx(c)) return rc;
+    prof_flush(c);
+    int k = 0;
+    for (auto &s : c->stats) {
+        if (k >= max) break;
+        if (stats) {
+            memset(&stats[k], 0, sizeof(nsg_kernel_stat));
+            strncpy(stats[k].name, s.name.c_str(), sizeof(stats[k].name) - 1);
+            stats[k].launches = s.launches;
+            stats[k].total_ms = s.total_ms;
+            stats[k].bytes = s.bytes;
+        }
+        k++;
+    }
+    if (count) *count = (int)c->stats.size();
+    return NSG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,184 @@
+// nsg_internal.cuh -- shared declarations of libnsg (context, buffers, device math).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "nsg.h"
+
+namespace nsg {
+
+constexpr int kMaxLevels = 64;        // adaptive levels N = 2^k, k < 64
+constexpr int kStatBins = 66;         // level histogram bins held on device
+constexpr int kLevelNotConverged = -1;
+constexpr int kLevelLcBase = 100;     // Levi-Civita particles record 100 + level
+constexpr int kLevelLcFallback = 99;
+constexpr int kRadixBits = 8;
+constexpr int kRadixBuckets = 1 << kRadixBits;
+constexpr int kRadixThreads = 256;
+constexpr int kRadixItems = 16;       // keys per thread per tile
+constexpr int kRadixTile = kRadixThreads * kRadixItems;
+constexpr int kReduceBlocks = 1024;   // fixed block count of energy partial sums
+
+// Device-resident counters and flags of one context (a single allocation).
+struct DevCounters {
+    unsigned int status;                    // NSG_ST_* bits
+    unsigned int lc_count;                  // particles routed to Levi-Civita
+    unsigned int qcount[kMaxLevels + 1];    // queue length per leapfrog level
+    unsigned long long level_hist[kStatBins];
+    double energy[2];                       // K, W of the last sort
+    double point_mass;                      // current central point mass
+    unsigned int bucket_overflow;           // near-sorted sort overflow flag
+    unsigned int pad;
+};
+
+struct KernelStat {
+    std::string name;
+    int64_t launches = 0;
+    double total_ms = 0.0;
+    double bytes = 0.0;
+};
+
+}  // namespace nsg
+
+struct nsg_ctx {
+    nsg_params p{};
+    cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;     // Levi-Civita work runs here, overlapped
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool own_stream = false;
+    int device = 0;
+    int num_sms = 0;
+    std::string err;
+
+    int64_t n = 0, cap = 0;
+    bool sorted = false;             // state is in (r, id) order with gnum/a0 valid
+    bool inv_valid = false;          // inv maps ids to the current array order
+    int64_t steps_done = 0;
+    int64_t launches = 0;            // kernels launched by steps/sorts (for reporting)
+
+    // state, two copies (sort source/destination)
+    double *r[2] = {nullptr, nullptr}, *vr[2] = {nullptr, nullptr}, *ell[2] = {nullptr, nullptr};
+    double *aux[2] = {nullptr, nullptr};
+    int32_t *id[2] = {nullptr, nullptr};
+    int cur = 0;                     // index of the live copy
+
+    double *a0 = nullptr;            // dv/dt at the step start, per sorted position
+    int32_t *inv = nullptr;          // id -> current index (the reference's inverse_map)
+    int8_t *level = nullptr;         // accepted level per particle
+
+    // radix sort scratch
+    uint64_t *keys[2] = {nullptr, nullptr};
+    uint32_t *vals[2] = {nullptr, nullptr};
+    uint32_t *tile_counts = nullptr; // [256][ntiles]
+    uint32_t *digit_tot = nullptr;   // [256]
+
+    // leapfrog level queues (ping-pong) and the Levi-Civita list
+    uint32_t *q_idx[2] = {nullptr, nullptr};
+    double *q_r[2] = {nullptr, nullptr}, *q_v[2] = {nullptr, nullptr};
+    uint32_t *lc_idx = nullptr;
+
+    double *red_part = nullptr;      // [2][kReduceBlocks] energy partials
+    nsg::DevCounters *ctr = nullptr; // device counters
+    nsg::DevCounters *h_ctr = nullptr; // pinned mirror
+
+    // staging for uploads of ids given as doubles
+    double *stage_d = nullptr;
+
+    bool profiling = false;
+    std::vector<nsg::KernelStat> stats;
+    std::vector<cudaEvent_t> ev_pool;
+};
+
+namespace nsg {
+
+// ---------------------------------------------------------------- device math
+// All integrator arithmetic uses explicit round-to-nearest intrinsics so that no
+// multiply-add is contracted: each operation rounds like the reference's C code
+// compiled with -ffp-contract=off.
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// -(G) * (i / n) * M (+ the point-mass term when present), nsphere.c:513.
+__device__ __forceinline__ double gnum_of(int64_t i, int64_t n, double G, double M, double Mpt)
+{
+    double g = dmul(dmul(-G, ddiv((double)i, (double)n)), M);
+    if (Mpt != 0.0) g = dsub(g, dmul(G, Mpt));
+    return g;
+}
+
+// gravity + centrifugal: gnum/(r*r) + l2/(r*r*r), nsphere.c:502-535.
+__device__ __forceinline__ double acc_leap(double r, double gnum, double l2)
+{
+    double r2 = dmul(r, r);
+    return dadd(ddiv(gnum, r2), ddiv(l2, dmul(r2, r)));
+}
+
+// Levi-Civita: gnum/(rho*rho) + l2/(rho*rho*rho*rho), nsphere.c:563-599, 1777-1787.
+__device__ __forceinline__ double acc_lc(double rho, double gnum, double l2)
+{
+    double p2 = dmul(rho, rho);
+    double p4 = dmul(dmul(p2, rho), rho);
+    return dadd(ddiv(gnum, p2), ddiv(l2, p4));
+}
+
+// Order-preserving map of a double to uint64: -0.0 -> +0.0, NaN -> all ones.
+__device__ __forceinline__ uint64_t radius_key(double r)
+{
+    if (r != r) return ~0ull;
+    unsigned long long u = (r == 0.0) ? 0ull : (unsigned long long)__double_as_longlong(r);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Appends one entry per active predicate to a queue; returns the slot or -1.
+__device__ __forceinline__ int warp_append(bool pred, unsigned int *counter)
+{
+    unsigned active = __activemask();
+    unsigned mask = __ballot_sync(active, pred);
+    if (!pred) return -1;
+    int leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    int lane = threadIdx.x & 31;
+    if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return (int)(base + __popc(mask & lanemask_lt()));
+}
+
+// ------------------------------------------------------------- host helpers
+int set_err(nsg_ctx *c, int code, const std::string &msg);
+int cuda_err(nsg_ctx *c, cudaError_t e, const char *what);
+int grid_for(nsg_ctx *c, int64_t n, int threads, int per_sm = 8);
+
+// Profiling: brackets a launch group with events when profiling is on.
+struct ProfScope {
+    nsg_ctx *c;
+    const char *name;
+    double bytes;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ProfScope(nsg_ctx *c_, const char *name_, double bytes_);
+    ~ProfScope();
+};
+void prof_flush(nsg_ctx *c);
+
+// kernels' host launchers (return NSG_OK or error)
+int sort_state(nsg_ctx *c);                           // radix sort + fused rank/force pass
+int integrate_adaptive(nsg_ctx *c);                   // method 3 / 5 on sorted state
+int kdk_first_half(nsg_ctx *c);                       // kick (old rank) + drift
+int kdk_second_half(nsg_ctx *c);                      // kick with new rank (a0)
+int finalize_energy(nsg_ctx *c);
+int launch_gather(nsg_ctx *c, const int32_t *d_ids, int k, double *d_out, int32_t *d_rank);
+int launch_level_hist(nsg_ctx *c);
+int launch_ids_from_double(nsg_ctx *c, const double *d_src, int32_t *d_dst, int64_t n);
+int launch_validate_ids(nsg_ctx *c, const int32_t *d_id, int64_t n, int *ok);
+
+}  // namespace nsg

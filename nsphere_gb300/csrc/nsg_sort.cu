@@ -1,0 +1,316 @@
+// nsg_sort.cu -- radial sort of the resident state by (r, id) and the fused
+// rank / enclosed-mass / force pass.
+//
+// Replaces sort_particles (nsphere.c:8605-8665, quadsort of the five columns by
+// r) plus the inverse_map rebuild (nsphere.c:5789-5794).  The enclosed mass of
+// the reference is the sorted rank, M_i = (i/N) M (nsphere.c:513); the pass after
+// the sort writes, per sorted position, the force at the step start
+// gnum_i/r^2 + ell^2/r^3 (nsphere.c:502-535), the inverse map and the energy
+// partial sums.
+//
+// Sort algorithm (general path): the permutation is seeded in id order (ids are a
+// permutation of 0..n-1), then an LSD radix sort over the 64-bit order-preserving
+// radius key, 8 bits per pass, stable.  Stability on an id-ordered start gives the
+// (r, id) total order.  Each pass: per-tile digit counts -> per-digit scan ->
+// stable warp-level ranking (match.any) and scatter.  No kernel waits on another
+// block, so no spin loops.
+#include "nsg_internal.cuh"
+
+namespace nsg {
+
+// Seeds the sort: keys[id] = key(r), vals[id] = source index.  Marks NaN radii.
+__global__ void k_seed_keys(const double *__restrict__ r, const int32_t *__restrict__ id,
+                            int64_t n, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
+                            DevCounters *ctr)
+{
+    bool nan_seen = false;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        double rk = r[k];
+        int32_t j = id[k];
+        nan_seen |= (rk != rk);
+        keys[j] = radius_key(rk);
+        vals[j] = (uint32_t)k;
+    }
+    if (nan_seen) atomicOr(&ctr->status, NSG_ST_NAN);
+}
+
+// Per-tile histogram of one digit.  counts is digit-major: counts[d * ntiles + t].
+__global__ void __launch_bounds__(kRadixThreads)
+k_tile_hist(const uint64_t *__restrict__ keys, int64_t n, int shift, int ntiles,
+            uint32_t *__restrict__ counts)
+{
+    __shared__ uint32_t h[kRadixBuckets];
+    for (int d = threadIdx.x; d < kRadixBuckets; d += blockDim.x) h[d] = 0;
+    __syncthreads();
+    int64_t base = (int64_t)blockIdx.x * kRadixTile;
+#pragma unroll 4
+    for (int j = 0; j < kRadixItems; j++) {
+        int64_t idx = base + j * kRadixThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(unsigned)(keys[idx] >> shift) & (kRadixBuckets - 1)], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadixBuckets; d += blockDim.x)
+        counts[(int64_t)d * ntiles + blockIdx.x] = h[d];
+}
+
+// Block-wide exclusive scan of one value per thread (blockDim.x == 1024).
+__device__ __forceinline__ uint32_t block_excl_scan_1024(uint32_t v, uint32_t *warp_tot,
+                                                         uint32_t *total)
+{
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t t = warp_tot[lane];
+        uint32_t s = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        warp_tot[lane] = s - t;
+        if (lane == 31) *total = s;
+    }
+    __syncthreads();
+    uint32_t r = warp_tot[w] + x - v;
+    __syncthreads();
+    return r;
+}
+
+// Sum of each digit's row of tile counts.  One block per digit.
+__global__ void __launch_bounds__(1024)
+k_digit_totals(const uint32_t *__restrict__ counts, int ntiles, uint32_t *__restrict__ tot)
+{
+    __shared__ uint32_t wsum[32];
+    const uint32_t *row = counts + (int64_t)blockIdx.x * ntiles;
+    uint32_t s = 0;
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) s += row[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = wsum[threadIdx.x];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) tot[blockIdx.x] = s;
+    }
+}
+
+// Turns each digit's row into global exclusive offsets: base(digit) + prefix over
+// tiles.  One block per digit.
+__global__ void __launch_bounds__(1024)
+k_digit_scan(uint32_t *__restrict__ counts, int ntiles, const uint32_t *__restrict__ tot)
+{
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t total;
+    __shared__ uint32_t base_s;
+    if (threadIdx.x == 0) {
+        uint32_t b = 0;
+        for (int d = 0; d < (int)blockIdx.x; d++) b += tot[d];
+        base_s = b;
+    }
+    __syncthreads();
+    uint32_t carry = base_s;
+    uint32_t *row = counts + (int64_t)blockIdx.x * ntiles;
+    for (int t0 = 0; t0 < ntiles; t0 += 1024) {
+        int t = t0 + threadIdx.x;
+        uint32_t v = (t < ntiles) ? row[t] : 0u;
+        uint32_t ex = block_excl_scan_1024(v, warp_tot, &total);
+        if (t < ntiles) row[t] = carry + ex;
+        carry += total;
+        __syncthreads();
+    }
+}
+
+// Stable ranking and scatter of one tile for one digit.  Warp w of the block owns
+// 512 consecutive keys; item j of lane l is key base + j*32 + l, so walking j and
+// then lanes visits the keys in input order and the match.any ranks are stable.
+__global__ void __launch_bounds__(kRadixThreads)
+k_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
+          uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n,
+          int shift, int ntiles, const uint32_t *__restrict__ offsets)
+{
+    constexpr int W = kRadixThreads / 32;
+    __shared__ uint32_t whist[W][kRadixBuckets];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < W * kRadixBuckets; d += blockDim.x) (&whist[0][0])[d] = 0;
+    __syncthreads();
+
+    const int64_t base = (int64_t)blockIdx.x * kRadixTile + (int64_t)w * (kRadixItems * 32);
+    const unsigned lt = lanemask_lt();
+    uint64_t k[kRadixItems];
+    uint32_t v[kRadixItems];
+    uint32_t rank[kRadixItems];
+    uint32_t dig[kRadixItems];
+#pragma unroll
+    for (int j = 0; j < kRadixItems; j++) {
+        int64_t idx = base + j * 32 + lane;
+        bool ok = idx < n;
+        k[j] = ok ? keys_in[idx] : 0ull;
+        v[j] = ok ? vals_in[idx] : 0u;
+        dig[j] = ok ? ((unsigned)(k[j] >> shift) & (kRadixBuckets - 1)) : (unsigned)kRadixBuckets;
+    }
+#pragma unroll
+    for (int j = 0; j < kRadixItems; j++) {
+        unsigned d = dig[j];
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        uint32_t cnt = 0;
+        if (d < kRadixBuckets) cnt = whist[w][d];
+        rank[j] = cnt + __popc(peers & lt);
+        __syncwarp();
+        if (d < kRadixBuckets && lane == __ffs(peers) - 1) whist[w][d] = cnt + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadixBuckets; d += blockDim.x) {
+        uint32_t run = offsets[(int64_t)d * ntiles + blockIdx.x];
+#pragma unroll
+        for (int ww = 0; ww < W; ww++) {
+            uint32_t t = whist[ww][d];
+            whist[ww][d] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRadixItems; j++) {
+        unsigned d = dig[j];
+        if (d < kRadixBuckets) {
+            uint32_t pos = whist[w][d] + rank[j];
+            keys_out[pos] = k[j];
+            vals_out[pos] = v[j];
+        }
+    }
+}
+
+// Gathers the state into sorted order and computes, per sorted position p:
+// the force numerator of rank p, the acceleration at the step start, the inverse
+// map, and the energy partial sums (fixed grid, fixed tree order: deterministic).
+template <bool AUX>
+__global__ void __launch_bounds__(256)
+k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
+                    const double *__restrict__ r0, const double *__restrict__ v0,
+                    const double *__restrict__ l0, const int32_t *__restrict__ id0,
+                    const double *__restrict__ x0,
+                    double *__restrict__ r1, double *__restrict__ v1, double *__restrict__ l1,
+                    int32_t *__restrict__ id1, double *__restrict__ x1,
+                    double *__restrict__ a0, int32_t *__restrict__ inv,
+                    double G, double M, const DevCounters *__restrict__ ctr,
+                    double *__restrict__ red_part)
+{
+    const double Mpt = ctr->point_mass;
+    const double m = M / (double)n;
+    double ek = 0.0, ew = 0.0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t s = perm[p];
+        double r = r0[s], v = v0[s], l = l0[s];
+        int32_t idv = id0[s];
+        r1[p] = r;
+        v1[p] = v;
+        l1[p] = l;
+        id1[p] = idv;
+        if (AUX) x1[p] = x0[s];
+        inv[idv] = (int32_t)p;
+        double gn = gnum_of(p, n, G, M, Mpt);
+        double l2 = dmul(l, l);
+        double r2 = dmul(r, r);
+        a0[p] = dadd(ddiv(gn, r2), ddiv(l2, dmul(r2, r)));
+        ek += 0.5 * m * (v * v + l2 / r2);
+        ew += m * gn / r;
+    }
+    // block reduction in a fixed order
+    __shared__ double sk[8], sw[8];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ek += __shfl_down_sync(0xffffffffu, ek, o);
+        ew += __shfl_down_sync(0xffffffffu, ew, o);
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { sk[w] = ek; sw[w] = ew; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) { a += sk[i]; b += sw[i]; }
+        red_part[blockIdx.x] = a;
+        red_part[kReduceBlocks + blockIdx.x] = b;
+    }
+}
+
+__global__ void k_finalize_energy(const double *__restrict__ red_part, int nblk, DevCounters *ctr)
+{
+    __shared__ double sk[32], sw[32];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < nblk; i += blockDim.x) { a += red_part[i]; b += red_part[kReduceBlocks + i]; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sk[threadIdx.x >> 5] = a; sw[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0.0, y = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) { x += sk[i]; y += sw[i]; }
+        ctr->energy[0] = x;
+        ctr->energy[1] = y;
+    }
+}
+
+int sort_state(nsg_ctx *c)
+{
+    const int64_t n = c->n;
+    const int src = c->cur, dst = 1 - c->cur;
+    const int ntiles = (int)((n + kRadixTile - 1) / kRadixTile);
+    cudaStream_t s = c->stream;
+    {
+        ProfScope ps(c, "sort_seed", (double)n * (8 + 4 + 8 + 4));
+        k_seed_keys<<<grid_for(c, n, 256), 256, 0, s>>>(c->r[src], c->id[src], n, c->keys[0],
+                                                         c->vals[0], c->ctr);
+    }
+    int kb = 0;
+    {
+        ProfScope ps(c, "sort_radix", (double)n * 8 * (8 + 12 + 12));
+        for (int pass = 0; pass < 8; pass++) {
+            int shift = pass * kRadixBits;
+            k_tile_hist<<<ntiles, kRadixThreads, 0, s>>>(c->keys[kb], n, shift, ntiles, c->tile_counts);
+            k_digit_totals<<<kRadixBuckets, 1024, 0, s>>>(c->tile_counts, ntiles, c->digit_tot);
+            k_digit_scan<<<kRadixBuckets, 1024, 0, s>>>(c->tile_counts, ntiles, c->digit_tot);
+            k_scatter<<<ntiles, kRadixThreads, 0, s>>>(c->keys[kb], c->vals[kb], c->keys[1 - kb],
+                                                       c->vals[1 - kb], n, shift, ntiles,
+                                                       c->tile_counts);
+            kb = 1 - kb;
+        }
+    }
+    {
+        ProfScope ps(c, "rank_force", (double)n * (4 + 28 + 28 + 8 + 4 + (c->p.carry_aux ? 16 : 0)));
+        if (c->p.carry_aux)
+            k_gather_rank_force<true><<<kReduceBlocks, 256, 0, s>>>(
+                c->vals[kb], n, c->r[src], c->vr[src], c->ell[src], c->id[src], c->aux[src],
+                c->r[dst], c->vr[dst], c->ell[dst], c->id[dst], c->aux[dst], c->a0, c->inv,
+                c->p.G, c->p.M_total, c->ctr, c->red_part);
+        else
+            k_gather_rank_force<false><<<kReduceBlocks, 256, 0, s>>>(
+                c->vals[kb], n, c->r[src], c->vr[src], c->ell[src], c->id[src], nullptr,
+                c->r[dst], c->vr[dst], c->ell[dst], c->id[dst], nullptr, c->a0, c->inv,
+                c->p.G, c->p.M_total, c->ctr, c->red_part);
+        k_finalize_energy<<<1, 1024, 0, s>>>(c->red_part, kReduceBlocks, c->ctr);
+    }
+    c->launches += 1 + 8 * 4 + 2;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(c, e, "sort kernels");
+    c->cur = dst;
+    c->sorted = true;
+    c->inv_valid = true;
+    return NSG_OK;
+}
+
+}  // namespace nsg

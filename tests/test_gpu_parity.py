@@ -1,0 +1,256 @@
+"""GPU parity: libnsg through its C ABI against the CPU oracle on identical inputs.
+
+Bar: bit equality (sort permutation, r, v_r, levels) at sizes the oracle runs in
+seconds, plus size-independent properties (sortedness, permutation, idempotence,
+energy) at the full workload size.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+from nsphere_gb300 import ics
+
+pytestmark = pytest.mark.gpu
+
+
+def _shuffle(seed, *cols):
+    perm = np.random.default_rng(seed).permutation(len(cols[0]))
+    return tuple(c[perm] for c in cols)
+
+
+def _ctx(nsg, **kw):
+    # a finite Levi-Civita tau-step cap bounds the worst-case kernel time; none of
+    # these cases comes near it, so results equal the oracle's (cap 1e8)
+    kw.setdefault("max_tau_steps", 1_000_000)
+    return nsg.Context(nsg.default_params(**kw))
+
+
+# ------------------------------------------------------------------ sort
+
+@pytest.mark.parametrize("n", [1, 2, 31, 4096, 4097, 100003])
+def test_sort_matches_oracle_random(nsg, oracle, n):
+    rng = np.random.default_rng(n)
+    r = rng.lognormal(0, 2, n)
+    vr, ell = rng.normal(size=n), rng.uniform(0, 1, n)
+    ids = rng.permutation(n).astype(np.int32)
+    with _ctx(nsg) as c:
+        c.upload(r, vr, ell, ids)
+        c.sort()
+        gr, gv, gl, gid = c.download()
+    orr, ov, ol, oid = oracle.sort(r, vr, ell, ids)
+    assert np.array_equal(gid, oid)
+    assert np.array_equal(gr, orr) and np.array_equal(gv, ov) and np.array_equal(gl, ol)
+
+
+def test_sort_edge_keys(nsg, oracle):
+    """ties (broken by id), -0.0 == +0.0, negative radii, inf, NaN last."""
+    rng = np.random.default_rng(9)
+    n = 50000
+    r = rng.choice(np.array([0.0, -0.0, 1.0, 2.5, -3.0, np.inf, 1e-300, 5e-324]), n)
+    r[rng.choice(n, 10, replace=False)] = np.nan
+    ids = rng.permutation(n).astype(np.int32)
+    z = np.zeros(n)
+    with _ctx(nsg) as c:
+        c.upload(r, z, z, ids)
+        c.sort()
+        gr, _, _, gid = c.download()
+        assert c.status() & nsg.ST_NAN
+    orr, _, _, oid = oracle.sort(r, z, z, ids)
+    assert np.array_equal(gid, oid)
+    assert np.array_equal(gr.view(np.uint64), orr.view(np.uint64))  # keeps -0.0 bits
+
+
+def test_sort_matches_golden(nsg):
+    g = golden("sort.npz")
+    with nsg.Context(nsg.default_params(carry_aux=1)) as c:
+        c.upload(g["r"], g["vr"], g["ell"], g["ids"], aux=g["mu"])
+        c.sort()
+        r, vr, ell, ids, mu = c.download(with_aux=True)
+    out = g["out"]
+    assert np.array_equal(r, out[0]) and np.array_equal(vr, out[1]) and np.array_equal(ell, out[2])
+    assert np.array_equal(ids, out[3].astype(np.int32)) and np.array_equal(mu, out[4])
+
+
+def test_sort_particles_dropin(nsg, oracle):
+    rng = np.random.default_rng(4)
+    n = 10000
+    tab = np.ascontiguousarray(np.stack([rng.uniform(0, 5, n), rng.normal(size=n), rng.uniform(0, 1, n),
+                                         rng.permutation(n).astype(np.float64), rng.uniform(-1, 1, n)]))
+    want = oracle.sort(tab[0], tab[1], tab[2], tab[3].astype(np.int32), tab[4])
+    with nsg.Context(nsg.default_params(carry_aux=1)) as c:
+        nsg.sort_particles(c, tab)
+    assert np.array_equal(tab[0], want[0]) and np.array_equal(tab[4], want[4])
+    assert np.array_equal(tab[3].astype(np.int32), want[3])
+
+
+def test_bad_ids_rejected(nsg):
+    n = 100
+    r = np.linspace(1, 2, n)
+    ids = np.arange(n)
+    ids[5] = 7  # duplicate
+    with _ctx(nsg) as c:
+        with pytest.raises(nsg.NsgError) as e:
+            c.upload(r, r, r, ids)
+        assert e.value.code == nsg.NSG_EIDS
+        with pytest.raises(nsg.NsgError):
+            c.upload(r, r, r, np.arange(n) + 0.5)
+
+
+# ------------------------------------------------------------------ steps
+
+def _adaptive_case(n, seed, lowl=0):
+    r, vr, ell, ids = ics.hernquist(n, seed=seed)
+    r, vr, ell, ids = _shuffle(seed, r, vr, ell, ids)
+    ell = ell.copy()
+    rng = np.random.default_rng(seed + 1)
+    if lowl:
+        k = rng.choice(n, lowl, replace=False)
+        ell[k] = rng.uniform(0, 1e-4, lowl)
+    inner = np.flatnonzero(r < 0.2)[:20]
+    ell[inner] = np.sqrt(40.0 * r[inner] ** 3 / (1.0 + r[inner]) ** 2)
+    return r, vr, ell, ids
+
+
+@pytest.mark.parametrize("lc_rule,lc_radius,dt,msub", [
+    (0, 1e-3, 5e-4, 128),      # reference r_crit rule
+    (1, 1e-1, 5e-4, 128),      # fixed radius rule (many Levi-Civita particles)
+    (0, 1e-3, 5e-3, 1 << 12),  # deeper levels
+    (2, 1e-3, 2e-2, 64),       # leapfrog only, level cap reached
+])
+def test_adaptive_step_bit_exact(nsg, oracle, lc_rule, lc_radius, dt, msub):
+    n = 20000
+    r, vr, ell, ids = _adaptive_case(n, 21, lowl=100)
+    with _ctx(nsg, dt=dt, max_subdiv=msub, lc_rule=lc_rule, lc_radius=lc_radius) as c:
+        c.upload(r, vr, ell, ids)
+        c.step(1)
+        gr, gv, gl, gid = c.download()
+        glv = c.levels()
+        hist = c.level_hist(10)
+    p = oracle.params(dt=dt, max_subdiv=msub, lc_rule=lc_rule, lc_radius=lc_radius)
+    orr, ov, ol, oid, olv, cap = oracle.step_adaptive(p, r, vr, ell, ids)
+    assert np.array_equal(gid, oid)
+    assert np.array_equal(glv, olv), "accepted levels differ"
+    bad = np.flatnonzero((gr != orr) | (gv != ov))
+    assert bad.size == 0, "first mismatches at %s: gpu %s oracle %s" % (
+        bad[:5], list(zip(gr[bad[:3]], gv[bad[:3]])), list(zip(orr[bad[:3]], ov[bad[:3]])))
+    assert hist.sum() == n
+    assert hist[-1] == np.sum(olv >= 99)
+
+
+def test_method5_matches_golden(nsg):
+    g = golden("steps.npz")
+    with _ctx(nsg, dt=float(g["dt5"]), max_subdiv=128, lc_rule=0) as c:
+        c.upload(g["r"], g["vr"], g["ell"], g["ids"])
+        c.step(1)
+        r, vr, ell, ids = c.download()
+        assert c.level_hist(10)[-1] > 0
+    t = g["method5_rcrit"]
+    assert np.array_equal(ids, t[3].astype(np.int32))
+    assert np.array_equal(r, t[0]) and np.array_equal(vr, t[1])
+
+
+def test_kdk_matches_golden_and_oracle(nsg, oracle):
+    g = golden("steps.npz")
+    s = g["kdk_start"]
+    with _ctx(nsg, dt=float(g["dt_kdk"]), method=nsg.METHOD_KDK) as c:
+        c.upload(s[0], s[1], s[2], s[3])
+        c.step(5)
+        r, vr, ell, ids = c.download()
+    t = g["kdk5"]
+    assert np.array_equal(ids, t[3].astype(np.int32))
+    assert np.array_equal(r, t[0]) and np.array_equal(vr, t[1])
+    # longer run against the oracle on a Plummer sphere
+    n = 30000
+    r0, v0, l0, i0 = ics.plummer(n, seed=1)
+    p = oracle.params(dt=1e-3)
+    cur = (r0, v0, l0, i0)
+    for _ in range(20):
+        cur = oracle.step_kdk(p, *cur)
+    with _ctx(nsg, dt=1e-3, method=nsg.METHOD_KDK) as c:
+        c.upload(r0, v0, l0, i0)
+        c.step(20)
+        r, vr, ell, ids = c.download()
+    assert np.array_equal(ids, cur[3]) and np.array_equal(r, cur[0]) and np.array_equal(vr, cur[1])
+
+
+def test_multi_step_adaptive(nsg, oracle):
+    n = 8000
+    r, vr, ell, ids = _adaptive_case(n, 33)
+    p = oracle.params(dt=1e-3, max_subdiv=128, lc_rule=1, lc_radius=3e-2)
+    cur = (r, vr, ell, ids)
+    for _ in range(10):
+        o = oracle.step_adaptive(p, *cur)
+        cur = o[:4]
+    with _ctx(nsg, dt=1e-3, max_subdiv=128, lc_rule=1, lc_radius=3e-2) as c:
+        c.upload(r, vr, ell, ids)
+        c.step(10)
+        gr, gv, gl, gid = c.download()
+    assert np.array_equal(gid, cur[3]) and np.array_equal(gr, cur[0]) and np.array_equal(gv, cur[1])
+
+
+def test_energy_and_gather(nsg, oracle):
+    n = 50000
+    r, vr, ell, ids = ics.plummer(n, seed=5)
+    r, vr, ell, ids = _shuffle(5, r, vr, ell, ids)
+    with _ctx(nsg) as c:
+        c.upload(r, vr, ell, ids)
+        K, W = c.energy()
+        sr, sv, sl, sid = c.download()
+        q = np.array([0, 1, 2, 17, n - 1], dtype=np.int32)
+        gr, gv, gl, rank = c.gather(q)
+    p = oracle.params()
+    oK, oW = oracle.energy(p, sr, sv, sl)
+    assert abs(K - oK) <= 1e-12 * abs(oK) and abs(W - oW) <= 1e-12 * abs(oW)
+    # virial ratio of an equilibrium Plummer sphere is close to 1
+    assert 0.9 < 2 * K / abs(W) < 1.1
+    assert np.array_equal(sid[rank], q)
+    assert np.array_equal(gr, sr[rank]) and np.array_equal(gv, sv[rank])
+
+
+def test_gather_before_any_sort(nsg):
+    n = 1000
+    rng = np.random.default_rng(0)
+    r = rng.uniform(0, 1, n)
+    ids = rng.permutation(n)
+    with _ctx(nsg) as c:
+        c.upload(r, r, r, ids)
+        gr, _, _, rank = c.gather(np.array([ids[10], ids[500]], dtype=np.int32))
+    assert list(rank) == [10, 500] and gr[0] == r[10]
+
+
+# ----------------------------------------------------------- large sizes
+
+def test_large_sort_properties(nsg):
+    """At the workload size: output sorted by (r, id), a permutation, idempotent."""
+    n = 10_000_000
+    r, vr, ell, ids = ics.hernquist(n, seed=2)
+    r, vr, ell, ids = _shuffle(2, r, vr, ell, ids)
+    with _ctx(nsg) as c:
+        c.upload(r, vr, ell, ids)
+        c.sort()
+        sr, sv, sl, sid = c.download()
+        c.sort()
+        sr2, _, _, sid2 = c.download()
+    assert np.all(np.diff(sr) >= 0)
+    eq = np.flatnonzero(np.diff(sr) == 0)
+    assert np.all(sid[eq] < sid[eq + 1])
+    assert np.array_equal(np.sort(sid), np.arange(n))
+    assert np.array_equal(sid, sid2) and np.array_equal(sr, sr2)
+    # the payload travelled with its key
+    src = np.empty(n, dtype=np.int64)
+    src[ids] = np.arange(n)
+    assert np.array_equal(sv, vr[src[sid]]) and np.array_equal(sl, ell[src[sid]])
+
+
+def test_large_step_energy_drift(nsg):
+    """N = 1e6 Hernquist, 20 adaptive steps: relative energy drift stays small."""
+    n = 1_000_000
+    r, vr, ell, ids = ics.hernquist(n, seed=2)
+    with _ctx(nsg, dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3) as c:
+        c.upload(r, vr, ell, ids)
+        E0 = sum(c.energy())
+        c.step(20)
+        E1 = sum(c.energy())
+        st = c.status()
+    assert abs(E1 - E0) / abs(E0) < 1e-4
+    assert not (st & nsg.ST_TAU_CAP)

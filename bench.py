@@ -250,7 +250,9 @@ def main():
         state = ics.hernquist(args.n, seed=2 + rank) if args.workload == "adaptive" else ics.plummer(args.n, seed=1 + rank)
     r, vr, ell, ids = state
     n = len(r)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream shared by the library and the timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     p = ns.default_params(**params)
     if args.sched == "learned":
         p.sched = ns.SCHED_LEARNED

@@ -437,12 +437,9 @@ int nsg_step(nsg_ctx *c, int nsteps)
             // the reference sorts once before its time loop (nsphere.c:5339-5342)
             if (!c->sorted) rc = sort_state(c);
             if (!rc) rc = kdk_first_half(c);
-            if (!rc) rc = sort_state(c);
-            if (!rc) rc = kdk_second_half(c);
+            if (!rc) rc = sort_state_kick(c);
         } else {
-            rc = sort_state(c);
-            if (!rc) rc = integrate_adaptive(c);
-            c->sorted = false;  // radii moved
+            rc = integrate_adaptive(c);
         }
         if (rc) return rc;
         if (c->p.point_mass_rate != 0.0) {
@@ -552,6 +549,7 @@ int nsg_energy(nsg_ctx *c, double *K, double *W)
     if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
     if (!c->sorted)
         if (int rc = sort_state(c)) return rc;
+    if (int rc = compute_energy(c)) return rc;
     cudaError_t e = cudaMemcpyAsync(c->h_ctr->energy, c->ctr->energy, 16, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "energy readback");

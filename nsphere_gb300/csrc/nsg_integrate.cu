@@ -20,8 +20,17 @@
 namespace nsg {
 
 struct StepArgs {
-    const double *r_in, *v_in, *ell, *a0;
-    double *r_out, *v_out;      // may alias r_in / v_in (in-place update)
+    // sorted copy: the fused gather writes start values here; every particle's
+    // final (r, v) overwrites them in place once its level is accepted
+    const double *r_in, *v_in, *ell;
+    double *a0;                 // written for queued particles only
+    double *r_out, *v_out;      // alias r_in / v_in
+    double *ell_out, *aux_out;
+    int32_t *id_out, *inv;
+    // unsorted source copy and the permutation from the radix sort
+    const uint32_t *perm;
+    const double *r_src, *v_src, *l_src, *aux_src;
+    const int32_t *id_src;
     int8_t *level;
     int64_t n;
     double G, M, dt, tol_r, tol_v;
@@ -37,23 +46,20 @@ struct StepArgs {
     uint32_t *q_idx[2];
     double *q_r[2], *q_v[2];
     uint32_t *lc_idx;
+    // Substep sizes of each pass, identical for every particle, computed once on
+    // the host with the same IEEE divisions as nsphere.c:1566-1577:
+    // coarse N=1: halfKick h/(2.0*1), midStep h/(1.0*1); fine N=2^k: h/(4.0*N), h/(2.0*N).
+    double hk_c0, ms_c0;
+    double hk_f[kMaxLevels], ms_f[kMaxLevels];
 };
 
-// Fine (fine=1) or coarse pass of the micro leapfrog, nsphere.c:1550-1607, with the
-// first acceleration a_first = acc(r_in) supplied.
-__device__ __forceinline__ void micro_leap(double r, double v, double l2, double gn, double h,
-                                           int64_t N, bool fine, double a_first,
+// Micro leapfrog, nsphere.c:1550-1607: half-kick, (pairs-1) drift-kick pairs, drift,
+// half-kick.  pairs = N (coarse, 2N+1 substeps) or 2N (fine, 4N+1 substeps); the
+// first acceleration a_first = acc(r_in) is supplied by the rank/force pass.
+__device__ __forceinline__ void micro_leap(double r, double v, double l2, double gn,
+                                           double hk, double ms, int64_t pairs, double a_first,
                                            double &r_out, double &v_out)
 {
-    double hk, ms;
-    if (!fine) {
-        hk = ddiv(h, dmul(2.0, (double)N));
-        ms = ddiv(h, dmul(1.0, (double)N));
-    } else {
-        hk = ddiv(h, dmul(4.0, (double)N));
-        ms = ddiv(h, dmul(2.0, (double)N));
-    }
-    const int64_t pairs = fine ? 2 * N : N;
     v = dadd(v, dmul(hk, a_first));
     for (int64_t pp = 1; pp <= pairs - 1; pp++) {
         r = dadd(r, dmul(ms, v));
@@ -100,26 +106,39 @@ __device__ __forceinline__ bool route_lc(const StepArgs &a, int64_t i, double r,
     return (r > 1.0e-30) && (r < r_crit);
 }
 
-// Level 0 for every sorted position; queues the rest.
-__global__ void __launch_bounds__(256) k_level0(StepArgs a)
+// Fused pass after the radix sort, per sorted position i: gather the particle
+// into sorted order, write the inverse map (nsphere.c:5789-5794), compute its
+// rank force numerator and start acceleration (nsphere.c:502-535), route it
+// (nsphere.c:5804-5822), and run adaptive level 0 (nsphere.c:1660-1700).  The
+// pass is FP64-bound, so the gather traffic hides under the arithmetic.
+template <bool AUX>
+__global__ void __launch_bounds__(256) k_gather_level0(StepArgs a)
 {
     const double Mpt = a.ctr->point_mass;
     const bool last = (a.nlev <= 1);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        double r = a.r_in[i], v = a.v_in[i], ell = a.ell[i];
+        const uint32_t s = a.perm[i];
+        double r = a.r_src[s], v = a.v_src[s], ell = a.l_src[s];
+        const int32_t idv = a.id_src[s];
+        a.ell_out[i] = ell;
+        a.id_out[i] = idv;
+        if (AUX) a.aux_out[i] = a.aux_src[s];
+        a.inv[idv] = (int32_t)i;
         bool lc = route_lc(a, i, r, ell);
         int slot = warp_append(lc, &a.ctr->lc_count);
         if (lc) {
+            a.r_out[i] = r;          // start values for the Levi-Civita kernel
+            a.v_out[i] = v;
             a.lc_idx[slot] = (uint32_t)i;
             continue;
         }
         double gn = gnum_of(i, a.n, a.G, a.M, Mpt);
         double l2 = dmul(ell, ell);
-        double af = a.a0[i];
+        double af = acc_leap(r, gn, l2);
         double rc, vc, rf, vf;
-        micro_leap(r, v, l2, gn, a.dt, 1, false, af, rc, vc);
-        micro_leap(r, v, l2, gn, a.dt, 1, true, af, rf, vf);
+        micro_leap(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
+        micro_leap(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
         bool ok = converged(rc, vc, rf, vf, a.tol_r, a.tol_v);
         bool bad = !(isfinite(rf) && isfinite(vf));
         bool done = ok || last || bad;
@@ -133,6 +152,9 @@ __global__ void __launch_bounds__(256) k_level0(StepArgs a)
         }
         int q = warp_append(!done, &a.ctr->qcount[1]);
         if (!done) {
+            a.r_out[i] = r;          // start values stay for the higher levels
+            a.v_out[i] = v;
+            a.a0[i] = af;
             a.q_idx[1][q] = (uint32_t)i;
             a.q_r[1][q] = rf;
             a.q_v[1][q] = vf;
@@ -148,7 +170,8 @@ __global__ void __launch_bounds__(256) k_level(StepArgs a, int k)
     const double Mpt = a.ctr->point_mass;
     const bool last = (k >= a.nlev - 1);
     const int qi = k & 1, qo = (k + 1) & 1;
-    const int64_t N = (int64_t)1 << k;
+    const int64_t pairs = (int64_t)2 << k;   // fine pass of N = 2^k: 2N pairs
+    const double hk = a.hk_f[k], ms = a.ms_f[k];
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < cnt;
          e += (int64_t)gridDim.x * blockDim.x) {
         uint32_t i = a.q_idx[qi][e];
@@ -157,7 +180,7 @@ __global__ void __launch_bounds__(256) k_level(StepArgs a, int k)
         double gn = gnum_of(i, a.n, a.G, a.M, Mpt);
         double l2 = dmul(ell, ell);
         double rf, vf;
-        micro_leap(r, v, l2, gn, a.dt, N, true, a.a0[i], rf, vf);
+        micro_leap(r, v, l2, gn, hk, ms, pairs, a.a0[i], rf, vf);
         bool ok = converged(rc, vc, rf, vf, a.tol_r, a.tol_v);
         bool bad = !(isfinite(rf) && isfinite(vf));
         bool done = ok || last || bad;
@@ -301,35 +324,30 @@ __global__ void __launch_bounds__(128) k_levi_civita(StepArgs a)
 // First half of the method-2 body (nsphere.c:5487-5505): kick with the rank of the
 // current order, then drift.
 __global__ void __launch_bounds__(256)
-k_kick_drift(double *__restrict__ r, double *__restrict__ v, const double *__restrict__ ell,
-             int64_t n, double G, double M, double dt, const DevCounters *__restrict__ ctr)
+k_kick_drift(double *__restrict__ r, double *__restrict__ v, const double *__restrict__ a0,
+             int64_t n, double dt)
 {
-    const double Mpt = ctr->point_mass;
+    // a0 is gnum_i/r^2 + ell^2/r^3 at the current radius and rank: the force the
+    // reference recomputes for this kick (same operands, same result).
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        double ri = r[i], li = ell[i];
-        double acc = acc_leap(ri, gnum_of(i, n, G, M, Mpt), dmul(li, li));
-        double vi = dadd(v[i], dmul(dmul(0.5, acc), dt));
+        double vi = dadd(v[i], dmul(dmul(0.5, a0[i]), dt));
         v[i] = vi;
-        r[i] = dadd(ri, dmul(vi, dt));
+        r[i] = dadd(r[i], dmul(vi, dt));
     }
-}
-
-// Second kick with the new rank (nsphere.c:5520-5531); a0 is that acceleration.
-__global__ void __launch_bounds__(256)
-k_kick(double *__restrict__ v, const double *__restrict__ a0, int64_t n, double dt)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x)
-        v[i] = dadd(v[i], dmul(dmul(0.5, a0[i]), dt));
 }
 
 static StepArgs make_args(nsg_ctx *c)
 {
+    // the fused pass reads copy `src` through c->perm and writes copy `dst`
     StepArgs a{};
-    const int s = c->cur;
+    const int src = c->cur, s = 1 - c->cur;
     a.r_in = c->r[s]; a.v_in = c->vr[s]; a.ell = c->ell[s]; a.a0 = c->a0;
     a.r_out = c->r[s]; a.v_out = c->vr[s];
+    a.ell_out = c->ell[s]; a.aux_out = c->aux[s]; a.id_out = c->id[s]; a.inv = c->inv;
+    a.perm = c->perm;
+    a.r_src = c->r[src]; a.v_src = c->vr[src]; a.l_src = c->ell[src]; a.aux_src = c->aux[src];
+    a.id_src = c->id[src];
     a.level = c->level;
     a.n = c->n;
     a.G = c->p.G; a.M = c->p.M_total; a.dt = c->p.dt;
@@ -338,6 +356,14 @@ static StepArgs make_args(nsg_ctx *c)
     int nlev = 0;
     for (int64_t N = 1; N <= c->p.max_subdiv && nlev < kMaxLevels - 1; N *= 2) nlev++;
     a.nlev = nlev;
+    const double h = c->p.dt;
+    a.hk_c0 = h / (2.0 * 1.0);
+    a.ms_c0 = h / (1.0 * 1.0);
+    for (int k = 0; k < kMaxLevels; k++) {
+        const double N = (double)((int64_t)1 << (k < 62 ? k : 62));
+        a.hk_f[k] = h / (4.0 * N);
+        a.ms_f[k] = h / (2.0 * N);
+    }
     a.out_type = c->p.out_type;
     a.method = c->p.method;
     a.lc_rule = c->p.lc_rule;
@@ -353,6 +379,7 @@ static StepArgs make_args(nsg_ctx *c)
 
 int integrate_adaptive(nsg_ctx *c)
 {
+    if (int rc = sort_perm(c)) return rc;
     StepArgs a = make_args(c);
     cudaStream_t s = c->stream;
     cudaError_t e;
@@ -361,10 +388,15 @@ int integrate_adaptive(nsg_ctx *c)
     if (e != cudaSuccess) return cuda_err(c, e, "memset queue counters");
     const int grid = grid_for(c, c->n, 256, 8);
     {
-        ProfScope ps(c, "leap_level0", (double)c->n * (8 * 4 + 16 + 1));
-        k_level0<<<grid, 256, 0, s>>>(a);
+        // algorithmic bytes: perm 4, gather r v ell id 28, write r v ell id 28, inv 4, level 1
+        ProfScope ps(c, "gather_level0", (double)c->n * (4 + 28 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)));
+        if (c->p.carry_aux) k_gather_level0<true><<<grid, 256, 0, s>>>(a);
+        else k_gather_level0<false><<<grid, 256, 0, s>>>(a);
         c->launches += 1;
     }
+    c->cur = 1 - c->cur;
+    c->inv_valid = true;
+    c->sorted = false;  // radii moved
     if (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF) {
         e = cudaEventRecord(c->ev_fork, s);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
@@ -392,21 +424,10 @@ int kdk_first_half(nsg_ctx *c)
 {
     const int s = c->cur;
     ProfScope ps(c, "kdk_kick_drift", (double)c->n * (24 + 16));
-    k_kick_drift<<<grid_for(c, c->n, 256), 256, 0, c->stream>>>(c->r[s], c->vr[s], c->ell[s], c->n,
-                                                               c->p.G, c->p.M_total, c->p.dt, c->ctr);
+    k_kick_drift<<<grid_for(c, c->n, 256), 256, 0, c->stream>>>(c->r[s], c->vr[s], c->a0, c->n, c->p.dt);
     c->launches += 1;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "kick_drift");
-}
-
-int kdk_second_half(nsg_ctx *c)
-{
-    const int s = c->cur;
-    ProfScope ps(c, "kdk_kick", (double)c->n * 24);
-    k_kick<<<grid_for(c, c->n, 256), 256, 0, c->stream>>>(c->vr[s], c->a0, c->n, c->p.dt);
-    c->launches += 1;
-    cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "kick");
 }
 
 }  // namespace nsg

@@ -73,6 +73,7 @@ struct nsg_ctx {
     uint32_t *vals[2] = {nullptr, nullptr};
     uint32_t *tile_counts = nullptr; // [256][ntiles]
     uint32_t *digit_tot = nullptr;   // [256]
+    uint32_t *perm = nullptr;        // result of sort_perm: source index per sorted position
 
     // leapfrog level queues (ping-pong) and the Levi-Civita list
     uint32_t *q_idx[2] = {nullptr, nullptr};
@@ -171,11 +172,12 @@ struct ProfScope {
 void prof_flush(nsg_ctx *c);
 
 // kernels' host launchers (return NSG_OK or error)
-int sort_state(nsg_ctx *c);                           // radix sort + fused rank/force pass
-int integrate_adaptive(nsg_ctx *c);                   // method 3 / 5 on sorted state
-int kdk_first_half(nsg_ctx *c);                       // kick (old rank) + drift
-int kdk_second_half(nsg_ctx *c);                      // kick with new rank (a0)
-int finalize_energy(nsg_ctx *c);
+int sort_perm(nsg_ctx *c);                            // radix sort of the live copy -> c->perm
+int sort_state(nsg_ctx *c);                           // sort_perm + gather with rank force (a0)
+int sort_state_kick(nsg_ctx *c);                      // same, plus the second half-kick (KDK)
+int integrate_adaptive(nsg_ctx *c);                   // method 3 / 5: sort_perm, then fused gather + levels
+int kdk_first_half(nsg_ctx *c);                       // kick (a0 of the current rank) + drift
+int compute_energy(nsg_ctx *c);                       // K, W of the sorted live copy
 int launch_gather(nsg_ctx *c, const int32_t *d_ids, int k, double *d_out, int32_t *d_rank);
 int launch_level_hist(nsg_ctx *c);
 int launch_ids_from_double(nsg_ctx *c, const double *d_src, int32_t *d_dst, int64_t n);

@@ -191,10 +191,12 @@ k_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ val
     }
 }
 
-// Gathers the state into sorted order and computes, per sorted position p:
-// the force numerator of rank p, the acceleration at the step start, the inverse
-// map, and the energy partial sums (fixed grid, fixed tree order: deterministic).
-template <bool AUX>
+// Gathers the state into sorted order and computes, per sorted position p, the
+// acceleration at the step start a0 = gnum_p/r^2 + ell^2/r^3 with the force
+// numerator of rank p (nsphere.c:502-535) and the inverse map (nsphere.c:5789-5794).
+// KICK applies the second half-kick of the fixed-step body with the new rank,
+// v += 0.5*a0*dt (nsphere.c:5520-5531), in the same pass.
+template <bool AUX, bool KICK>
 __global__ void __launch_bounds__(256)
 k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
                     const double *__restrict__ r0, const double *__restrict__ v0,
@@ -203,31 +205,43 @@ k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
                     double *__restrict__ r1, double *__restrict__ v1, double *__restrict__ l1,
                     int32_t *__restrict__ id1, double *__restrict__ x1,
                     double *__restrict__ a0, int32_t *__restrict__ inv,
-                    double G, double M, const DevCounters *__restrict__ ctr,
-                    double *__restrict__ red_part)
+                    double G, double M, double dt, const DevCounters *__restrict__ ctr)
 {
     const double Mpt = ctr->point_mass;
-    const double m = M / (double)n;
-    double ek = 0.0, ew = 0.0;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
          p += (int64_t)gridDim.x * blockDim.x) {
         uint32_t s = perm[p];
         double r = r0[s], v = v0[s], l = l0[s];
         int32_t idv = id0[s];
+        double gn = gnum_of(p, n, G, M, Mpt);
+        double acc = acc_leap(r, gn, dmul(l, l));
+        if (KICK) v = dadd(v, dmul(dmul(0.5, acc), dt));
         r1[p] = r;
         v1[p] = v;
         l1[p] = l;
         id1[p] = idv;
         if (AUX) x1[p] = x0[s];
         inv[idv] = (int32_t)p;
-        double gn = gnum_of(p, n, G, M, Mpt);
-        double l2 = dmul(l, l);
-        double r2 = dmul(r, r);
-        a0[p] = dadd(ddiv(gn, r2), ddiv(l2, dmul(r2, r)));
-        ek += 0.5 * m * (v * v + l2 / r2);
-        ew += m * gn / r;
+        a0[p] = acc;
     }
-    // block reduction in a fixed order
+}
+
+// Energy partial sums of a sorted state: K = sum 1/2 m (v^2 + ell^2/r^2),
+// W = sum m gnum_i / r_i.  Fixed grid and tree order: deterministic.
+__global__ void __launch_bounds__(256)
+k_energy(const double *__restrict__ r, const double *__restrict__ v, const double *__restrict__ l,
+         int64_t n, double G, double M, const DevCounters *__restrict__ ctr, double *__restrict__ red_part)
+{
+    const double Mpt = ctr->point_mass;
+    const double m = M / (double)n;
+    double ek = 0.0, ew = 0.0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        double rr = r[p], vv = v[p], ll = l[p];
+        double gn = gnum_of(p, n, G, M, Mpt);
+        ek += 0.5 * m * (vv * vv + (ll * ll) / (rr * rr));
+        ew += m * gn / rr;
+    }
     __shared__ double sk[8], sw[8];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -265,10 +279,11 @@ __global__ void k_finalize_energy(const double *__restrict__ red_part, int nblk,
     }
 }
 
-int sort_state(nsg_ctx *c)
+// Radix sort of the live copy by (r, id); leaves the permutation in c->perm.
+int sort_perm(nsg_ctx *c)
 {
     const int64_t n = c->n;
-    const int src = c->cur, dst = 1 - c->cur;
+    const int src = c->cur;
     const int ntiles = (int)((n + kRadixTile - 1) / kRadixTile);
     cudaStream_t s = c->stream;
     {
@@ -290,27 +305,57 @@ int sort_state(nsg_ctx *c)
             kb = 1 - kb;
         }
     }
-    {
-        ProfScope ps(c, "rank_force", (double)n * (4 + 28 + 28 + 8 + 4 + (c->p.carry_aux ? 16 : 0)));
-        if (c->p.carry_aux)
-            k_gather_rank_force<true><<<kReduceBlocks, 256, 0, s>>>(
-                c->vals[kb], n, c->r[src], c->vr[src], c->ell[src], c->id[src], c->aux[src],
-                c->r[dst], c->vr[dst], c->ell[dst], c->id[dst], c->aux[dst], c->a0, c->inv,
-                c->p.G, c->p.M_total, c->ctr, c->red_part);
-        else
-            k_gather_rank_force<false><<<kReduceBlocks, 256, 0, s>>>(
-                c->vals[kb], n, c->r[src], c->vr[src], c->ell[src], c->id[src], nullptr,
-                c->r[dst], c->vr[dst], c->ell[dst], c->id[dst], nullptr, c->a0, c->inv,
-                c->p.G, c->p.M_total, c->ctr, c->red_part);
-        k_finalize_energy<<<1, 1024, 0, s>>>(c->red_part, kReduceBlocks, c->ctr);
-    }
-    c->launches += 1 + 8 * 4 + 2;
+    c->perm = c->vals[kb];
+    c->launches += 1 + 8 * 4;
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_err(c, e, "sort kernels");
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "sort kernels");
+}
+
+static int gather(nsg_ctx *c, bool kick)
+{
+    const int64_t n = c->n;
+    const int src = c->cur, dst = 1 - c->cur;
+    cudaStream_t s = c->stream;
+    ProfScope ps(c, kick ? "gather_kick" : "rank_force",
+                 (double)n * (4 + 28 + 28 + 8 + 4 + (c->p.carry_aux ? 16 : 0)));
+    const int grid = grid_for(c, n, 256, 8);
+#define NSG_GATHER(AUXV, KICKV)                                                                   \
+    k_gather_rank_force<AUXV, KICKV><<<grid, 256, 0, s>>>(                                        \
+        c->perm, n, c->r[src], c->vr[src], c->ell[src], c->id[src], c->aux[src], c->r[dst],      \
+        c->vr[dst], c->ell[dst], c->id[dst], c->aux[dst], c->a0, c->inv, c->p.G, c->p.M_total,   \
+        c->p.dt, c->ctr)
+    if (c->p.carry_aux) { if (kick) NSG_GATHER(true, true); else NSG_GATHER(true, false); }
+    else { if (kick) NSG_GATHER(false, true); else NSG_GATHER(false, false); }
+#undef NSG_GATHER
+    c->launches += 1;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(c, e, "gather kernel");
     c->cur = dst;
     c->sorted = true;
     c->inv_valid = true;
     return NSG_OK;
+}
+
+int sort_state(nsg_ctx *c)
+{
+    if (int rc = sort_perm(c)) return rc;
+    return gather(c, false);
+}
+
+int sort_state_kick(nsg_ctx *c)
+{
+    if (int rc = sort_perm(c)) return rc;
+    return gather(c, true);
+}
+
+int compute_energy(nsg_ctx *c)
+{
+    const int s = c->cur;
+    k_energy<<<kReduceBlocks, 256, 0, c->stream>>>(c->r[s], c->vr[s], c->ell[s], c->n, c->p.G,
+                                                   c->p.M_total, c->ctr, c->red_part);
+    k_finalize_energy<<<1, 1024, 0, c->stream>>>(c->red_part, kReduceBlocks, c->ctr);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "energy kernels");
 }
 
 }  // namespace nsg

@@ -161,6 +161,14 @@ int nsg_sync(nsg_ctx *ctx, int timeout_ms);
 int nsg_status(nsg_ctx *ctx, uint32_t *flags);
 int nsg_clear_status(nsg_ctx *ctx);
 
+/* Diagnostic without a reference counterpart: compares the library's integer-pipe
+ * double division (used by every integrator in place of the FP64 pipe's) with the
+ * hardware IEEE division on `count` generated operand pairs on the current device.
+ * mismatches must come back 0; fast_path counts pairs that took the integer path;
+ * first_bad[0..1] receives the first mismatching (a, b). */
+int nsg_selftest_division(uint64_t seed, int64_t count, int64_t *mismatches,
+                          int64_t *fast_path, double *first_bad);
+
 /* Kernels launched by steps and sorts so far, and steps taken (for reporting). */
 int nsg_counters(nsg_ctx *ctx, int64_t *launches, int64_t *steps);
 

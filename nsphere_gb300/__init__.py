@@ -30,6 +30,7 @@ EXPORTS = [
     "nsg_sort", "nsg_download", "nsg_download_particles", "nsg_device_state",
     "nsg_sort_particles", "nsg_gather", "nsg_energy", "nsg_level_hist", "nsg_levels",
     "nsg_sync", "nsg_status", "nsg_clear_status", "nsg_profile", "nsg_profile_read", "nsg_counters",
+    "nsg_selftest_division",
 ]
 
 
@@ -87,6 +88,7 @@ def lib() -> C.CDLL:
         "nsg_clear_status": [P],
         "nsg_profile": [P, C.c_int],
         "nsg_counters": [P, C.POINTER(I64), C.POINTER(I64)],
+        "nsg_selftest_division": [C.c_uint64, I64, C.POINTER(I64), C.POINTER(I64), P],
         "nsg_profile_read": [P, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)],
     }
     for name, args in sig.items():
@@ -235,6 +237,17 @@ class Context:
         self._check(self._L.nsg_profile_read(self._h, arr, 64, C.byref(cnt)))
         return [dict(name=arr[i].name.decode(), launches=arr[i].launches,
                      total_ms=arr[i].total_ms, bytes=arr[i].bytes) for i in range(min(cnt.value, 64))]
+
+
+def selftest_division(count: int, seed: int = 1):
+    """(mismatches, fast_path_count, first_bad_pair) of the integer-pipe division
+    against the hardware IEEE division on the current GPU."""
+    mism, fast = C.c_int64(), C.c_int64()
+    first = np.zeros(2)
+    rc = lib().nsg_selftest_division(seed, count, C.byref(mism), C.byref(fast), _ptr(first))
+    if rc != NSG_OK:
+        raise NsgError(rc, lib().nsg_last_error(None).decode())
+    return mism.value, fast.value, tuple(first)
 
 
 def sort_particles(ctx: Context, particles: np.ndarray):

@@ -167,6 +167,49 @@ __global__ void k_advance_point_mass(DevCounters *ctr, double rate_dt)
     ctr->point_mass += rate_dt;
 }
 
+__device__ __forceinline__ uint64_t mix64(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// Compares div_rn with the hardware IEEE division on `count` generated operand
+// pairs of eight classes: random normals, few-bit and all-ones mantissas, equal
+// mantissas, exact products, raw bit patterns (zero/subnormal/inf/NaN), and
+// exponents at the edges of the normal range.
+__global__ void k_selftest_div(uint64_t seed, int64_t count, unsigned long long *out, double *first)
+{
+    unsigned long long fast = 0;
+    const uint64_t MANT = (1ull << 52) - 1;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t h1 = mix64(seed ^ (uint64_t)(2 * k)), h2 = mix64(seed ^ (uint64_t)(2 * k + 1));
+        uint64_t h3 = mix64(h1 ^ h2);
+        int cls = (int)(k & 7);
+        uint64_t ea = 1023 + (h3 & 511) - 256, eb = 1023 + ((h3 >> 9) & 511) - 256;
+        uint64_t ma = h1 & MANT, mb = h2 & MANT;
+        if (cls == 1) mb &= ~((1ull << 40) - 1);
+        if (cls == 2) { ma |= MANT ^ 0xff; mb = h2 & 0xff; }
+        if (cls == 3) ma = mb;
+        if (cls == 6) { ea = (h3 >> 20) & 2047; eb = (h3 >> 31) & 2047; }
+        if (cls == 7) { ea = (h3 & 1) ? 1 + (h3 >> 40 & 63) : 2046 - (h3 >> 40 & 63); }
+        uint64_t ua = ((h3 >> 62) << 63) | (ea << 52) | ma, ub = (eb << 52) | mb;
+        double a = __longlong_as_double((long long)ua), b = __longlong_as_double((long long)ub);
+        if (cls == 4) a = __dmul_rn(b, (double)((h1 >> 40) + 1));
+        if (cls == 5) { a = __longlong_as_double((long long)(h1 >> 1)); b = __longlong_as_double((long long)(h2 >> 1)); }
+        double q;
+        bool f = div_rn_fast(a, b, &q);
+        if (!f) q = __ddiv_rn(a, b);
+        double t = __ddiv_rn(a, b);
+        fast += f;
+        bool same = (__double_as_longlong(q) == __double_as_longlong(t)) || (q != q && t != t);
+        if (!same && atomicAdd(&out[1], 1ull) == 0) { first[0] = a; first[1] = b; }
+    }
+    atomicAdd(&out[2], fast);
+}
+
 }  // namespace nsg
 
 using namespace nsg;
@@ -627,6 +670,36 @@ int nsg_clear_status(nsg_ctx *c)
     cudaError_t e = cudaMemsetAsync(&c->ctr->status, 0, 4, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "status clear");
+    return NSG_OK;
+}
+
+int nsg_selftest_division(uint64_t seed, int64_t count, int64_t *mismatches, int64_t *fast_path,
+                          double *first_bad)
+{
+    if (count < 0 || !mismatches) return set_err(nullptr, NSG_EINVAL, "bad selftest arguments");
+    unsigned long long *d_out = nullptr;
+    double *d_first = nullptr;
+    cudaError_t e = cudaMalloc((void **)&d_out, 3 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_first, 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(d_out, 0, 3 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(d_first, 0, 2 * sizeof(double));
+    if (e == cudaSuccess) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        k_selftest_div<<<sms * 8, 256>>>(seed, count, d_out, d_first);
+        e = cudaDeviceSynchronize();
+    }
+    unsigned long long h[3] = {0, 0, 0};
+    double f[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, d_out, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(f, d_first, sizeof(f), cudaMemcpyDeviceToHost);
+    cudaFree(d_out);
+    cudaFree(d_first);
+    if (e != cudaSuccess) return cuda_err(nullptr, e, "division selftest");
+    *mismatches = (int64_t)h[1];
+    if (fast_path) *fast_path = (int64_t)h[2];
+    if (first_bad) { first_bad[0] = f[0]; first_bad[1] = f[1]; }
     return NSG_OK;
 }
 

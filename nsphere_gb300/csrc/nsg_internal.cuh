@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "nsg.h"
+#include "nsg_div.cuh"
 
 namespace nsg {
 
@@ -101,7 +102,8 @@ namespace nsg {
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+// Division runs on the integer/FP32 pipes (nsg_div.cuh), bit-identical to IEEE.
+__device__ __forceinline__ double ddiv(double a, double b) { return div_rn(a, b); }
 
 // -(G) * (i / n) * M (+ the point-mass term when present), nsphere.c:513.
 __device__ __forceinline__ double gnum_of(int64_t i, int64_t n, double G, double M, double Mpt)

@@ -254,3 +254,14 @@ def test_large_step_energy_drift(nsg):
         st = c.status()
     assert abs(E1 - E0) / abs(E0) < 1e-4
     assert not (st & nsg.ST_TAU_CAP)
+
+
+def test_integer_pipe_division_matches_ieee(nsg):
+    """The integrators divide on the integer/FP32 pipes; every result must carry the
+    same bits as the hardware IEEE division."""
+    total = 0
+    for seed in (1, 2, 3):
+        mism, fast, first = nsg.selftest_division(200_000_000, seed=seed)
+        assert mism == 0, "first mismatch a=%r b=%r" % first
+        total += fast
+    assert total > 0.5 * 600_000_000  # most pairs take the integer path

@@ -225,6 +225,7 @@ static void free_buffers(nsg_ctx *c)
     }
     f(c->a0); f(c->inv); f(c->level); f(c->tile_counts); f(c->digit_tot); f(c->lc_idx);
     f(c->red_part); f(c->stage_d);
+    f(c->split); f(c->bcnt); f(c->boff); f(c->bkey); f(c->bpay);
     c->cap = 0;
 }
 
@@ -247,6 +248,9 @@ static int ensure_capacity(nsg_ctx *c, int64_t n)
     A(c->a0, d8); A(c->inv, d4); A(c->level, (size_t)n);
     A(c->tile_counts, (size_t)ntiles * kRadixBuckets * 4); A(c->digit_tot, kRadixBuckets * 4);
     A(c->lc_idx, d4); A(c->red_part, 2 * kReduceBlocks * 8); A(c->stage_d, d8);
+    const size_t nb = (size_t)((n + kBucketTarget - 1) / kBucketTarget);
+    A(c->split, nb * 8); A(c->bcnt, nb * 4); A(c->boff, nb * 4);
+    A(c->bkey, nb * kBucketCap * 8); A(c->bpay, nb * kBucketCap * 8);
     if (e != cudaSuccess) {
         free_buffers(c);
         return cuda_err(c, e, "device allocation");
@@ -268,6 +272,9 @@ static int check_params(nsg_ctx *c, const nsg_params *p)
     if (p->method != NSG_METHOD_KDK && p->method != NSG_METHOD_ADAPTIVE && p->method != NSG_METHOD_ADAPTIVE_LC)
         return set_err(c, NSG_EINVAL, "unknown method");
     if (p->max_subdiv < 1) return set_err(c, NSG_EINVAL, "max_subdiv must be >= 1");
+    // one warp holds every level of a Levi-Civita tau-step: levels + 2 <= 32 lanes
+    if (p->max_subdiv > (1LL << 29))
+        return set_err(c, NSG_EINVAL, "max_subdiv above 2^29 is not supported (reference default 2^28)");
     if (p->out_type < 0 || p->out_type > 2) return set_err(c, NSG_EINVAL, "out_type must be 0, 1 or 2");
     if (p->lc_rule < 0 || p->lc_rule > 2) return set_err(c, NSG_EINVAL, "unknown lc_rule");
     if (p->max_tau_steps < 0) return set_err(c, NSG_EINVAL, "max_tau_steps must be >= 0");
@@ -329,6 +336,7 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->ctr, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMemset(c->ctr, 0, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_ctr, sizeof(DevCounters));
+    if (e == cudaSuccess && bucket_setup(c) != NSG_OK) e = cudaErrorInvalidValue;
     if (e == cudaSuccess && p->point_mass != 0.0)
         e = cudaMemcpy(&c->ctr->point_mass, &p->point_mass, sizeof(double), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -414,6 +422,7 @@ static int upload_common(nsg_ctx *c, int64_t n)
     c->cur = 0;
     c->sorted = false;
     c->inv_valid = false;
+    c->split_valid = false;
     return NSG_OK;
 }
 

@@ -1,0 +1,342 @@
+// nsg_bucket.cu -- near-sorted bucket sort: the fast path of the radial sort.
+//
+// Between steps every particle moves a small distance in r, so the state arrives
+// almost in (r, id) order.  The sort exploits that instead of re-sorting all 64
+// key bits (nsphere.c relies on the same property: quadsort is adaptive to
+// ordered runs, README "nearly N log N or even linear"):
+//
+//   splitters  S[b] = key(r) at sorted position b*B of the previous sort (written
+//              by the pass that consumed that sort), so S is non-decreasing;
+//   scatter    each particle finds its bucket b (S[b] <= key < S[b+1]) by a short
+//              search from its home bucket i/B, and appends (key, id, index) to a
+//              fixed-capacity bucket slot array;
+//   scan       exclusive scan of the bucket counts; a count above the capacity
+//              sets the fallback flag, and the general radix sort runs instead;
+//   sort       one block per bucket sorts its entries in registers/shared memory
+//              by a stable LSD radix over only the key bits that differ inside
+//              the bucket (typically 40 of 64), then by id where keys tie, and
+//              writes the source index of each sorted position.
+// The concatenation of sorted buckets is the (r, id) order: buckets partition the
+// key range in splitter order and equal keys share a bucket.
+#include "nsg_internal.cuh"
+
+namespace nsg {
+
+constexpr int kBucketThreads = 512;
+constexpr int kBucketItems = 12;
+constexpr int kBucketWarps = kBucketThreads / 32;
+constexpr int kSeg = kBucketItems * 32;      // positions owned by one warp
+
+// Largest b with S[b] <= key (S[0] is the smallest key), searched from home.
+__device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int nb, uint64_t key, int home)
+{
+    int b = home;
+    if (S[b] <= key) {
+        int steps = 0;
+        while (b + 1 < nb && S[b + 1] <= key && steps < 8) { b++; steps++; }
+        if (b + 1 < nb && S[b + 1] <= key) {       // far move: binary search in (b, nb)
+            int lo = b + 1, hi = nb - 1;           // S[lo] <= key
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (S[mid] <= key) lo = mid; else hi = mid - 1;
+            }
+            b = lo;
+        }
+    } else {
+        int steps = 0;
+        while (b > 0 && S[b] > key && steps < 8) { b--; steps++; }
+        if (S[b] > key) {                          // binary search in [0, b)
+            int lo = 0, hi = b - 1;                // S[0] <= key always
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (S[mid] <= key) lo = mid; else hi = mid - 1;
+            }
+            b = lo;
+        }
+    }
+    return b;
+}
+
+__global__ void __launch_bounds__(256)
+k_bucket_scatter(const double *__restrict__ r, const int32_t *__restrict__ id, int64_t n,
+                 const uint64_t *__restrict__ S, int nb, int B, int cap,
+                 unsigned int *__restrict__ cnt, uint64_t *__restrict__ bkey,
+                 uint64_t *__restrict__ bpay, DevCounters *ctr)
+{
+    bool nan_seen = false;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        double rp = r[p];
+        nan_seen |= (rp != rp);
+        uint64_t key = radius_key(rp);
+        int home = (int)(p / B);
+        if (home >= nb) home = nb - 1;
+        int b = find_bucket(S, nb, key, home);
+        unsigned active = __activemask();
+        unsigned peers = __match_any_sync(active, b);
+        int leader = __ffs(peers) - 1;
+        unsigned base = 0;
+        if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(&cnt[b], (unsigned)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        unsigned slot = base + __popc(peers & lanemask_lt());
+        if (slot < (unsigned)cap) {
+            int64_t at = (int64_t)b * cap + slot;
+            bkey[at] = key;
+            bpay[at] = ((uint64_t)(uint32_t)id[p] << 32) | (uint64_t)(uint32_t)p;
+        }
+    }
+    if (nan_seen) atomicOr(&ctr->status, NSG_ST_NAN);
+}
+
+// Exclusive scan of the bucket counts (one block); flags overflow.
+__global__ void __launch_bounds__(1024)
+k_bucket_scan(const unsigned int *__restrict__ cnt, int nb, int cap, unsigned int *__restrict__ off,
+              DevCounters *ctr)
+{
+    __shared__ unsigned int wt[32];
+    __shared__ unsigned int carry_s;
+    __shared__ int over_s;
+    if (threadIdx.x == 0) { carry_s = 0; over_s = 0; }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int t0 = 0; t0 < nb; t0 += 1024) {
+        int t = t0 + threadIdx.x;
+        unsigned v = t < nb ? cnt[t] : 0u;
+        if (v > (unsigned)cap) over_s = 1;
+        unsigned x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wt[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            unsigned s = wt[lane], tot = s;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned y = __shfl_up_sync(0xffffffffu, tot, o);
+                if (lane >= o) tot += y;
+            }
+            wt[lane] = tot - s;
+        }
+        __syncthreads();
+        if (t < nb) off[t] = carry_s + wt[w] + x - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry_s += wt[w] + x;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ctr->need_fallback = over_s ? 1u : 0u;
+        if (over_s) atomicOr(&ctr->status, NSG_ST_SORT_FALLBACK);
+    }
+}
+
+// One stable LSD pass on 8 bits of the key chosen by `digit_of`, over the block's
+// items held in registers (warp w owns positions [w*kSeg, (w+1)*kSeg), item j of
+// lane l is position w*kSeg + j*32 + l).  Items are exchanged through shared memory.
+template <typename DigitFn>
+__device__ __forceinline__ void block_radix_pass(uint64_t (&k)[kBucketItems], uint64_t (&v)[kBucketItems],
+                                                 DigitFn digit_of, uint32_t (*whist)[256],
+                                                 uint32_t *dtot, uint64_t *xk)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = lanemask_lt();
+    for (int d = threadIdx.x; d < kBucketWarps * 256; d += blockDim.x) (&whist[0][0])[d] = 0;
+    __syncthreads();
+    uint32_t rd[kBucketItems];   // (rank within warp and digit) << 8 | digit
+#pragma unroll
+    for (int j = 0; j < kBucketItems; j++) {
+        unsigned d = digit_of(k[j], v[j]);
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        uint32_t c = whist[w][d];
+        rd[j] = ((c + __popc(peers & lt)) << 8) | d;
+        __syncwarp();
+        if (lane == __ffs(peers) - 1) whist[w][d] = c + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // digit-major exclusive offsets: per digit over warps, then over digits
+    if (threadIdx.x < 256) {
+        const int d = threadIdx.x;
+        uint32_t run = 0;
+#pragma unroll
+        for (int ww = 0; ww < kBucketWarps; ww++) {
+            uint32_t t = whist[ww][d];
+            whist[ww][d] = run;
+            run += t;
+        }
+        dtot[d] = run;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // scan of 256 digit totals by one warp: 8 per lane
+        uint32_t loc[8], s = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) { loc[q] = dtot[lane * 8 + q]; s += loc[q]; }
+        uint32_t x = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        uint32_t run = x - s;
+#pragma unroll
+        for (int q = 0; q < 8; q++) { dtot[lane * 8 + q] = run; run += loc[q]; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kBucketItems; j++) {
+        const uint32_t d = rd[j] & 255u;
+        uint32_t pos = dtot[d] + whist[w][d] + (rd[j] >> 8);
+        xk[pos] = k[j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kBucketItems; j++) k[j] = xk[w * kSeg + j * 32 + lane];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kBucketItems; j++) {
+        const uint32_t d = rd[j] & 255u;
+        uint32_t pos = dtot[d] + whist[w][d] + (rd[j] >> 8);
+        xk[pos] = v[j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kBucketItems; j++) v[j] = xk[w * kSeg + j * 32 + lane];
+    __syncthreads();
+}
+
+__device__ __forceinline__ uint64_t block_reduce_u64(uint64_t x, bool is_min, uint64_t *red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        uint64_t y = __shfl_xor_sync(0xffffffffu, x, o);
+        x = is_min ? (y < x ? y : x) : (y > x ? y : x);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = x;
+    __syncthreads();
+    x = red[0];
+    for (int i = 1; i < kBucketWarps; i++) {
+        uint64_t y = red[i];
+        x = is_min ? (y < x ? y : x) : (y > x ? y : x);
+    }
+    return x;
+}
+
+__global__ void __launch_bounds__(kBucketThreads)
+k_bucket_sort(const unsigned int *__restrict__ cnt, const unsigned int *__restrict__ off, int cap,
+              const uint64_t *__restrict__ bkey, const uint64_t *__restrict__ bpay,
+              uint32_t *__restrict__ perm, const DevCounters *__restrict__ ctr)
+{
+    if (ctr->need_fallback) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint64_t *xk = reinterpret_cast<uint64_t *>(smem);                      // cap * 8
+    uint32_t(*whist)[256] = reinterpret_cast<uint32_t(*)[256]>(xk + cap);   // warps * 256 * 4
+    uint32_t *dtot = &whist[kBucketWarps - 1][0] + 256;                      // 256 * 4
+    __shared__ uint64_t red[kBucketWarps];
+
+    const int b = blockIdx.x;
+    const uint32_t m = cnt[b];
+    const uint32_t base = off[b];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t src0 = (int64_t)b * cap;
+    uint64_t k[kBucketItems], v[kBucketItems];
+    uint64_t kmin = ~0ull, kmax = 0ull;
+#pragma unroll
+    for (int j = 0; j < kBucketItems; j++) {
+        uint32_t pos = w * kSeg + j * 32 + lane;
+        bool ok = pos < m;
+        k[j] = ok ? bkey[src0 + pos] : ~0ull;
+        v[j] = ok ? bpay[src0 + pos] : ~0ull;
+        if (ok) { kmin = k[j] < kmin ? k[j] : kmin; kmax = k[j] > kmax ? k[j] : kmax; }
+    }
+    if (m == 0) return;
+    kmin = block_reduce_u64(kmin, true, red);
+    kmax = block_reduce_u64(kmax, false, red);
+    const uint64_t diff = kmin ^ kmax;
+    const int kbits = diff ? 64 - __clzll((long long)diff) : 0;
+    for (int shift = 0; shift < kbits; shift += 8)
+        block_radix_pass(k, v, [shift](uint64_t kk, uint64_t) { return (unsigned)(kk >> shift) & 255u; },
+                         whist, dtot, xk);
+    // ties on the key (equal radii) are ordered by id: re-sort by id, then by key
+    int tie = 0;
+    {
+        // after the passes item (w, j, lane) sits at position w*kSeg + j*32 + lane
+#pragma unroll
+        for (int j = 0; j < kBucketItems; j++) xk[w * kSeg + j * 32 + lane] = k[j];
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kBucketItems; j++) {
+            uint32_t pos = w * kSeg + j * 32 + lane;
+            if (pos + 1 < m && xk[pos] == xk[pos + 1]) tie = 1;
+        }
+        tie = __syncthreads_or(tie);
+    }
+    if (tie) {
+        uint64_t imin = ~0ull, imax = 0ull;
+#pragma unroll
+        for (int j = 0; j < kBucketItems; j++) {
+            uint32_t pos = w * kSeg + j * 32 + lane;
+            if (pos < m) { uint64_t x = v[j] >> 32; imin = x < imin ? x : imin; imax = x > imax ? x : imax; }
+        }
+        imin = block_reduce_u64(imin, true, red);
+        imax = block_reduce_u64(imax, false, red);
+        const uint64_t idiff = imin ^ imax;
+        const int ibits = idiff ? 64 - __clzll((long long)idiff) : 0;
+        for (int shift = 0; shift < ibits; shift += 8)
+            block_radix_pass(k, v, [shift](uint64_t, uint64_t vv) { return (unsigned)((vv >> 32) >> shift) & 255u; },
+                             whist, dtot, xk);
+        for (int shift = 0; shift < kbits; shift += 8)
+            block_radix_pass(k, v, [shift](uint64_t kk, uint64_t) { return (unsigned)(kk >> shift) & 255u; },
+                             whist, dtot, xk);
+    }
+#pragma unroll
+    for (int j = 0; j < kBucketItems; j++) {
+        uint32_t pos = w * kSeg + j * 32 + lane;
+        if (pos < m) perm[base + pos] = (uint32_t)(v[j] & 0xffffffffu);
+    }
+}
+
+size_t bucket_smem_bytes(int cap)
+{
+    return (size_t)cap * 8 + (size_t)kBucketWarps * 256 * 4 + 256 * 4;
+}
+
+// Fast path of the sort.  Returns NSG_OK having launched the bucket kernels; the
+// radix kernels that follow run only if the scan flagged an overflow.
+int bucket_sort_perm(nsg_ctx *c)
+{
+    const int64_t n = c->n;
+    const int src = c->cur;
+    const int B = kBucketTarget, cap = kBucketCap;
+    const int nb = (int)((n + B - 1) / B);
+    cudaStream_t s = c->stream;
+    cudaError_t e = cudaMemsetAsync(c->bcnt, 0, (size_t)nb * 4, s);
+    if (e != cudaSuccess) return cuda_err(c, e, "bucket count reset");
+    {
+        ProfScope ps(c, "bucket_scatter", (double)n * (8 + 4 + 16));
+        k_bucket_scatter<<<grid_for(c, n, 256, 8), 256, 0, s>>>(c->r[src], c->id[src], n, c->split, nb, B,
+                                                                 cap, c->bcnt, c->bkey, c->bpay, c->ctr);
+        k_bucket_scan<<<1, 1024, 0, s>>>(c->bcnt, nb, cap, c->boff, c->ctr);
+    }
+    {
+        ProfScope ps(c, "bucket_sort", (double)n * (16 + 4));
+        k_bucket_sort<<<nb, kBucketThreads, bucket_smem_bytes(cap), s>>>(c->bcnt, c->boff, cap, c->bkey,
+                                                                        c->bpay, c->vals[0], c->ctr);
+    }
+    c->launches += 3;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "bucket sort kernels");
+}
+
+int bucket_setup(nsg_ctx *c)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_bucket_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bucket_smem_bytes(kBucketCap));
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "bucket sort attribute");
+}
+
+}  // namespace nsg

@@ -1,40 +1,48 @@
 // nsg_integrate.cu -- per-particle integrators of the step, on the sorted state.
 //
-// Adaptive leapfrog (nsphere.c:1550-1735) as per-level work queues:
-//   level 0 runs for every particle (coarse N=1 and fine N=1);
-//   level k >= 1 runs only for the particles queued by level k-1.
-// Two facts keep the results bit-identical to the reference's loop:
+// Adaptive leapfrog (nsphere.c:1550-1735).  The reference tries N = 1, 2, 4, ...
+// and returns at the first N whose coarse (2N+1 substeps) and fine (4N+1
+// substeps) passes agree.  Three facts let the GPU reorganise that loop while
+// returning bit-identical results:
 //   * every level restarts from the step's initial (r, v) (nsphere.c:1673-1684),
-//     so a particle at level k needs only its inputs;
-//   * the coarse pass of level k (2N'+1 substeps, N' = 2^k) performs exactly the
-//     operations of the fine pass of level k-1 (4N+1 substeps, N = 2^(k-1)):
-//     halfKick h/(2N') = h/(4N) and midStep h/N' = h/(2N).  The queue therefore
-//     carries the previous fine result and level k computes only its fine pass.
-// The first force of every pass is the force at (r_in, rank) that the rank/force
-// pass already wrote (a0), as every pass starts with the same half-kick at r_in.
-//
-// Levi-Civita particles (nsphere.c:1990-2334) are listed by level 0 and integrated
-// on a side stream, overlapped with the leapfrog levels.
+//     so levels are independent of one another;
+//   * the coarse pass of level k (N' = 2^k: halfKick h/(2N'), midStep h/N',
+//     N' pairs) performs exactly the operations of the fine pass of level k-1
+//     (N = 2^(k-1): halfKick h/(4N), midStep h/(2N), 2N pairs), so each level
+//     needs only its own fine pass;
+//   * every pass starts with the same half-kick at r_in, so the first force is
+//     computed once.
+// Work split:
+//   k_gather_level0  fused with the sort's gather: level 0 for every particle
+//                    (throughput-bound; divisions on the integer pipe);
+//   k_levels_lanes   particles that failed level 0: a group of lanes per
+//                    particle, lane j computing the fine pass of level j+1 at the
+//                    same time; the group stops at the first level that agrees
+//                    with the level below (latency-bound; FP64-pipe divisions).
+// Adaptive Levi-Civita (nsphere.c:1990-2334): one warp per particle, started on a
+// side stream right after the sort, overlapped with the leapfrog work.  Within a
+// tau-step the lanes compute the coarse N=1 pass, the fine pass of every level and
+// the non-converged fallback pass at once; the first converging level decides.
+// The force at the end of one substep is the force at the start of the next
+// (nsphere.c:2014 and :2022 evaluate forceLCfun at the same rho), so it is
+// evaluated once.
 #include "nsg_internal.cuh"
 
 namespace nsg {
 
 struct StepArgs {
-    // sorted copy: the fused gather writes start values here; every particle's
-    // final (r, v) overwrites them in place once its level is accepted
-    const double *r_in, *v_in, *ell;
-    double *a0;                 // written for queued particles only
-    double *r_out, *v_out;      // alias r_in / v_in
-    double *ell_out, *aux_out;
+    // sorted copy: k_gather_level0 writes it; final (r, v) land in r_out / v_out
+    double *r_out, *v_out, *ell_out, *aux_out;
     int32_t *id_out, *inv;
-    // unsorted source copy and the permutation from the radix sort
+    double *a0;                 // start acceleration, written for queued particles only
+    uint64_t *split;            // splitters of the next near-sorted sort
+    // unsorted source copy and the permutation from the sort
     const uint32_t *perm;
     const double *r_src, *v_src, *l_src, *aux_src;
     const int32_t *id_src;
     int8_t *level;
     int64_t n;
     double G, M, dt, tol_r, tol_v;
-    int64_t max_subdiv;
     int nlev;                   // number of levels: floor(log2(max_subdiv)) + 1
     int out_type;
     int method;
@@ -43,19 +51,21 @@ struct StepArgs {
     int N_taumin;
     int64_t max_tau_steps;
     DevCounters *ctr;
-    uint32_t *q_idx[2];
-    double *q_r[2], *q_v[2];
+    uint32_t *q_idx;            // particles that failed level 0
+    double *q_r, *q_v;          // their fine N=1 result (the coarse pass of level 1)
     uint32_t *lc_idx;
     // Substep sizes of each pass, identical for every particle, computed once on
-    // the host with the same IEEE divisions as nsphere.c:1566-1577:
-    // coarse N=1: halfKick h/(2.0*1), midStep h/(1.0*1); fine N=2^k: h/(4.0*N), h/(2.0*N).
+    // the host with the same IEEE divisions as nsphere.c:1566-1577 (exact here:
+    // h divided by powers of two): coarse N=1 halfKick h/2, midStep h;
+    // fine N=2^k halfKick h/(4N), midStep h/(2N).
     double hk_c0, ms_c0;
     double hk_f[kMaxLevels], ms_f[kMaxLevels];
 };
 
 // Micro leapfrog, nsphere.c:1550-1607: half-kick, (pairs-1) drift-kick pairs, drift,
 // half-kick.  pairs = N (coarse, 2N+1 substeps) or 2N (fine, 4N+1 substeps); the
-// first acceleration a_first = acc(r_in) is supplied by the rank/force pass.
+// first acceleration a_first = acc(r_in) is passed in.
+template <bool HW>
 __device__ __forceinline__ void micro_leap(double r, double v, double l2, double gn,
                                            double hk, double ms, int64_t pairs, double a_first,
                                            double &r_out, double &v_out)
@@ -63,19 +73,22 @@ __device__ __forceinline__ void micro_leap(double r, double v, double l2, double
     v = dadd(v, dmul(hk, a_first));
     for (int64_t pp = 1; pp <= pairs - 1; pp++) {
         r = dadd(r, dmul(ms, v));
-        v = dadd(v, dmul(ms, acc_leap(r, gn, l2)));
+        v = dadd(v, dmul(ms, acc_leap<HW>(r, gn, l2)));
     }
     r = dadd(r, dmul(ms, v));
-    v = dadd(v, dmul(hk, acc_leap(r, gn, l2)));
+    v = dadd(v, dmul(hk, acc_leap<HW>(r, gn, l2)));
     r_out = r;
     v_out = v;
 }
 
+// Acceptance test of nsphere.c:1688-1691 (and :2125-2128, whose radius term is
+// scaled by rF^2 instead of rF).
+template <bool HW>
 __device__ __forceinline__ bool converged(double rc, double vc, double rf, double vf,
-                                          double tol_r, double tol_v)
+                                          double rscale, double tol_r, double tol_v)
 {
-    double dr = ddiv(fabs(dsub(rf, rc)), dadd(fabs(rf), 1.0e-30));
-    double dv = ddiv(fabs(dsub(vf, vc)), dadd(fabs(vf), 1.0e-30));
+    double dr = ddivx<HW>(fabs(dsub(rf, rc)), dadd(fabs(rscale), 1.0e-30));
+    double dv = ddivx<HW>(fabs(dsub(vf, vc)), dadd(fabs(vf), 1.0e-30));
     return (dr < tol_r) && (dv < tol_v);
 }
 
@@ -106,11 +119,12 @@ __device__ __forceinline__ bool route_lc(const StepArgs &a, int64_t i, double r,
     return (r > 1.0e-30) && (r < r_crit);
 }
 
-// Fused pass after the radix sort, per sorted position i: gather the particle
-// into sorted order, write the inverse map (nsphere.c:5789-5794), compute its
-// rank force numerator and start acceleration (nsphere.c:502-535), route it
-// (nsphere.c:5804-5822), and run adaptive level 0 (nsphere.c:1660-1700).  The
-// pass is FP64-bound, so the gather traffic hides under the arithmetic.
+// Fused pass after the sort, per sorted position i: gather the particle into
+// sorted order, write the inverse map (nsphere.c:5789-5794) and the next sort's
+// splitter, then -- unless it is routed to Levi-Civita (nsphere.c:5804-5822),
+// which the side stream handles -- compute its rank force numerator and start
+// acceleration (nsphere.c:502-535) and run adaptive level 0.  The pass is
+// FP64-bound, so the gather traffic hides under the arithmetic.
 template <bool AUX>
 __global__ void __launch_bounds__(256) k_gather_level0(StepArgs a)
 {
@@ -119,29 +133,23 @@ __global__ void __launch_bounds__(256) k_gather_level0(StepArgs a)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t s = a.perm[i];
-        double r = a.r_src[s], v = a.v_src[s], ell = a.l_src[s];
+        const double r = a.r_src[s], v = a.v_src[s], ell = a.l_src[s];
         const int32_t idv = a.id_src[s];
         a.ell_out[i] = ell;
         a.id_out[i] = idv;
         if (AUX) a.aux_out[i] = a.aux_src[s];
         a.inv[idv] = (int32_t)i;
-        bool lc = route_lc(a, i, r, ell);
-        int slot = warp_append(lc, &a.ctr->lc_count);
-        if (lc) {
-            a.r_out[i] = r;          // start values for the Levi-Civita kernel
-            a.v_out[i] = v;
-            a.lc_idx[slot] = (uint32_t)i;
-            continue;
-        }
-        double gn = gnum_of(i, a.n, a.G, a.M, Mpt);
-        double l2 = dmul(ell, ell);
-        double af = acc_leap(r, gn, l2);
+        write_splitter(a.split, i, r);
+        if (route_lc(a, i, r, ell)) continue;
+        const double gn = gnum_of(i, a.n, a.G, a.M, Mpt);
+        const double l2 = dmul(ell, ell);
+        const double af = acc_leap(r, gn, l2);
         double rc, vc, rf, vf;
-        micro_leap(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
-        micro_leap(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
-        bool ok = converged(rc, vc, rf, vf, a.tol_r, a.tol_v);
-        bool bad = !(isfinite(rf) && isfinite(vf));
-        bool done = ok || last || bad;
+        micro_leap<false>(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
+        micro_leap<false>(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
+        const bool ok = converged<false>(rc, vc, rf, vf, rf, a.tol_r, a.tol_v);
+        const bool bad = !(isfinite(rf) && isfinite(vf));
+        const bool done = ok || last || bad;
         if (done) {
             double ro, vo;
             select_out(a.out_type, rc, vc, rf, vf, ro, vo);
@@ -150,119 +158,123 @@ __global__ void __launch_bounds__(256) k_gather_level0(StepArgs a)
             a.level[i] = ok ? 0 : kLevelNotConverged;
             if (!ok) atomicOr(&a.ctr->status, bad ? (NSG_ST_NAN | NSG_ST_NOT_CONVERGED) : NSG_ST_NOT_CONVERGED);
         }
-        int q = warp_append(!done, &a.ctr->qcount[1]);
+        const int q = warp_append(!done, &a.ctr->qcount[1]);
         if (!done) {
-            a.r_out[i] = r;          // start values stay for the higher levels
+            a.r_out[i] = r;          // start values for the higher levels
             a.v_out[i] = v;
             a.a0[i] = af;
-            a.q_idx[1][q] = (uint32_t)i;
-            a.q_r[1][q] = rf;
-            a.q_v[1][q] = vf;
+            a.q_idx[q] = (uint32_t)i;
+            a.q_r[q] = rf;
+            a.q_v[q] = vf;
         }
     }
 }
 
-// Level k >= 1 over the entries queued by level k-1.
-__global__ void __launch_bounds__(256) k_level(StepArgs a, int k)
+// Levels 1 .. nlev-1 for the particles queued by level 0.  A group of G lanes
+// (G = a power of two >= nlev-1) serves one particle; lane j runs the fine pass of
+// level k = j+1 (2^(k+1) drift-kick pairs).  All lanes advance one pair per
+// iteration, so level k's pass ends at iteration 2^(k+1): its test then uses the
+// pass of level k-1 (lane j-1, or the queued level-0 result for k = 1), in the
+// reference's order, and the group stops at the first level that passes.
+__global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
 {
-    const unsigned cnt = a.ctr->qcount[k];
+    const unsigned cnt = a.ctr->qcount[1];
     if (cnt == 0) return;
     const double Mpt = a.ctr->point_mass;
-    const bool last = (k >= a.nlev - 1);
-    const int qi = k & 1, qo = (k + 1) & 1;
-    const int64_t pairs = (int64_t)2 << k;   // fine pass of N = 2^k: 2N pairs
-    const double hk = a.hk_f[k], ms = a.ms_f[k];
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < cnt;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t i = a.q_idx[qi][e];
-        double rc = a.q_r[qi][e], vc = a.q_v[qi][e];
-        double r = a.r_in[i], v = a.v_in[i], ell = a.ell[i];
-        double gn = gnum_of(i, a.n, a.G, a.M, Mpt);
-        double l2 = dmul(ell, ell);
-        double rf, vf;
-        micro_leap(r, v, l2, gn, hk, ms, pairs, a.a0[i], rf, vf);
-        bool ok = converged(rc, vc, rf, vf, a.tol_r, a.tol_v);
-        bool bad = !(isfinite(rf) && isfinite(vf));
-        bool done = ok || last || bad;
-        if (done) {
-            double ro, vo;
-            select_out(a.out_type, rc, vc, rf, vf, ro, vo);
-            a.r_out[i] = ro;
-            a.v_out[i] = vo;
-            a.level[i] = ok ? (int8_t)k : (int8_t)kLevelNotConverged;
-            if (!ok) atomicOr(&a.ctr->status, bad ? (NSG_ST_NAN | NSG_ST_NOT_CONVERGED) : NSG_ST_NOT_CONVERGED);
+    const int lane = threadIdx.x & 31;
+    const int j = lane & (G - 1);              // this lane runs level j+1
+    const int g0 = lane & ~(G - 1);            // first lane of the group
+    const int groups_per_warp = 32 / G;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int nl = a.nlev - 1;                 // levels run here
+    const bool mine = j < nl;
+    const int k = j + 1;
+    const int64_t pairs = mine ? ((int64_t)2 << k) : 0;
+    const double hk = mine ? a.hk_f[k] : 0.0, ms = mine ? a.ms_f[k] : 0.0;
+    for (int64_t round = 0;; round++) {
+        const int64_t e = (round * warps + gw) * groups_per_warp + (lane / G);
+        if (__all_sync(0xffffffffu, e >= (int64_t)cnt)) break;
+        const bool have = e < (int64_t)cnt;
+        uint32_t i = 0;
+        double v_in = 0.0, l2 = 0.0, gn = 0.0, af = 0.0, rq = 0.0, vq = 0.0, r = 0.0;
+        if (have) {
+            i = a.q_idx[e];
+            r = a.r_out[i];
+            v_in = a.v_out[i];
+            const double ell = a.ell_out[i];
+            l2 = dmul(ell, ell);
+            gn = gnum_of<true>(i, a.n, a.G, a.M, Mpt);
+            af = a.a0[i];
+            rq = a.q_r[e];
+            vq = a.q_v[e];
         }
-        int q = warp_append(!done, &a.ctr->qcount[k + 1]);
-        if (!done) {
-            a.q_idx[qo][q] = i;
-            a.q_r[qo][q] = rf;
-            a.q_v[qo][q] = vf;
+        bool active = have;                    // the group is still searching
+        double v = dadd(v_in, dmul(hk, af));
+        double rf = 0.0, vf = 0.0;             // this lane's finished pass
+        int64_t it = 0;
+        int kcheck = 1;                        // next level to test
+        while (__any_sync(0xffffffffu, active)) {
+            // one drift-kick pair; the last pair of a pass ends with the half-kick
+            if (active && it < pairs) {
+                r = dadd(r, dmul(ms, v));
+                if (it + 1 < pairs) v = dadd(v, dmul(ms, acc_leap<true>(r, gn, l2)));
+                else { v = dadd(v, dmul(hk, acc_leap<true>(r, gn, l2))); rf = r; vf = v; }
+            }
+            it++;
+            // level kcheck's pass (lane kcheck-1 of the group) ended at it = 2^(kcheck+1)
+            if (kcheck <= nl && it == ((int64_t)2 << kcheck)) {
+                const int srcF = g0 + kcheck - 1;
+                const int srcC = kcheck > 1 ? srcF - 1 : srcF;
+                const double rF = __shfl_sync(0xffffffffu, rf, srcF);
+                const double vF = __shfl_sync(0xffffffffu, vf, srcF);
+                const double rC0 = __shfl_sync(0xffffffffu, rf, srcC);
+                const double vC0 = __shfl_sync(0xffffffffu, vf, srcC);
+                const double rC = (kcheck == 1) ? rq : rC0;
+                const double vC = (kcheck == 1) ? vq : vC0;
+                if (active) {
+                    const bool ok = converged<true>(rC, vC, rF, vF, rF, a.tol_r, a.tol_v);
+                    const bool bad = !(isfinite(rF) && isfinite(vF));
+                    if (ok || bad || kcheck == nl) {
+                        if (j == 0) {
+                            double ro, vo;
+                            select_out(a.out_type, rC, vC, rF, vF, ro, vo);
+                            a.r_out[i] = ro;
+                            a.v_out[i] = vo;
+                            a.level[i] = ok ? (int8_t)kcheck : (int8_t)kLevelNotConverged;
+                            if (!ok) atomicOr(&a.ctr->status, bad ? (NSG_ST_NAN | NSG_ST_NOT_CONVERGED)
+                                                                  : NSG_ST_NOT_CONVERGED);
+                        }
+                        active = false;
+                    }
+                }
+                kcheck++;
+            }
         }
     }
 }
 
 // ---------------------------------------------------------- Levi-Civita path
 
-// subSteps tau-leapfrog substeps over h_tau, nsphere.c:1990-2036.
-__device__ __forceinline__ void micro_lc(double rho, double v, double t, int64_t subSteps,
-                                         double h_tau, double gn, double l2,
-                                         double &rho_o, double &v_o, double &t_o)
+// Lists the Levi-Civita particles of the sorted order (the routing of
+// k_gather_level0); runs on the side stream right after the sort.
+__global__ void __launch_bounds__(256) k_lc_select(StepArgs a)
 {
-    const double dtau = ddiv(h_tau, (double)subSteps);
-    const double hdt = dmul(0.5, dtau);
-    for (int64_t ss = 0; ss < subSteps; ss++) {
-        double f1 = acc_lc(rho, gn, l2);
-        double vh = dadd(v, dmul(hdt, f1));
-        double rn = dadd(rho, dmul(dtau, dmul(dmul(0.5, rho), vh)));
-        double f2 = acc_lc(rn, gn, l2);
-        double vn = dadd(vh, dmul(hdt, f2));
-        double rm = dmul(0.5, dadd(rho, rn));
-        t = dadd(t, dmul(dtau, dmul(rm, rm)));
-        rho = rn;
-        v = vn;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = a.perm[i];
+        const bool lc = route_lc(a, i, a.r_src[s], a.l_src[s]);
+        const int slot = warp_append(lc, &a.ctr->lc_count);
+        if (lc) a.lc_idx[slot] = (uint32_t)i;
     }
-    rho_o = rho; v_o = v; t_o = t;
 }
 
-// One adaptive tau-step, nsphere.c:2077-2186.  The coarse pass of level k is the
-// fine pass of level k-1 (same substep count over the same h_tau).  Returns the
-// accepted level or -1 (fallback fine pass at 4*(2*N_last)+1 substeps).
-__device__ int tau_step_lc(double rho, double v, double t, double hg, double tol_r,
-                           double tol_v, int nlev, double gn, double l2, int out_type,
-                           double &rho_o, double &v_o, double &t_o)
-{
-    double rC, vC, tC, rF, vF, tF;
-    micro_lc(rho, v, t, 3, hg, gn, l2, rC, vC, tC);
-    int64_t N = 1;
-    for (int k = 0; k < nlev; k++, N *= 2) {
-        micro_lc(rho, v, t, 4 * N + 1, hg, gn, l2, rF, vF, tF);
-        double rsq = dmul(rF, rF);
-        double drho = ddiv(fabs(dsub(rF, rC)), dadd(fabs(rsq), 1.0e-30));
-        double dv = ddiv(fabs(dsub(vF, vC)), dadd(fabs(vF), 1.0e-30));
-        if (drho < tol_r && dv < tol_v) {
-            if (out_type == 0) { rho_o = rC; v_o = vC; t_o = tC; }
-            else if (out_type == 1) { rho_o = rF; v_o = vF; t_o = tF; }
-            else {
-                double rr = dsub(dmul(4.0, rF), dmul(3.0, rC));
-                double vr = dsub(dmul(4.0, vF), dmul(3.0, vC));
-                double tr = dsub(dmul(4.0, tF), dmul(3.0, tC));
-                if (rr < 0.0) rr = 0.0;
-                rho_o = rr; v_o = vr; t_o = tr;
-            }
-            return k;
-        }
-        if (!(isfinite(rF) && isfinite(vF))) break;
-        rC = rF; vC = vF; tC = tF;
-    }
-    // after the loop N = 2^nlev = 2 * N_last
-    micro_lc(rho, v, t, 4 * N + 1, hg, gn, l2, rho_o, v_o, t_o);
-    return -1;
-}
-
-// Adaptive full Levi-Civita step, nsphere.c:2231-2334.  Entries are spread so
-// that consecutive particles land on different warps: each is a long serial
-// chain, and one per warp keeps lanes from waiting on one another.
-__global__ void __launch_bounds__(128) k_levi_civita(StepArgs a)
+// One warp per Levi-Civita particle (nsphere.c:2231-2334).  Lane roles in each
+// adaptive tau-step (nsphere.c:2077-2186): lane 0 the coarse N=1 pass (3
+// substeps), lane 1+k the fine pass of level k (4*2^k+1 substeps; it is also the
+// coarse pass of level k+1), lane nlev+1 the fallback fine pass at N = 2^nlev.
+// Requires nlev + 2 <= 32 (max_subdiv < 2^30, checked by the host).
+__global__ void __launch_bounds__(128) k_levi_civita_lanes(StepArgs a)
 {
     const unsigned cnt = a.ctr->lc_count;
     if (cnt == 0) return;
@@ -270,35 +282,94 @@ __global__ void __launch_bounds__(128) k_levi_civita(StepArgs a)
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    for (int64_t e = (int64_t)lane * warps + gw; e < cnt; e += 32 * warps) {
-        uint32_t i = a.lc_idx[e];
-        double r_in = a.r_in[i], v_in = a.v_in[i], ell = a.ell[i];
-        double gn = gnum_of(i, a.n, a.G, a.M, Mpt);
+    const int nlev = a.nlev;
+    int64_t my_sub = 0;                        // substeps of this lane's pass (0: idle)
+    if (lane == 0) my_sub = 3;
+    else if (lane <= nlev) my_sub = 4 * ((int64_t)1 << (lane - 1)) + 1;
+    else if (lane == nlev + 1) my_sub = 4 * ((int64_t)1 << nlev) + 1;
+    const int64_t fb_sub = 4 * ((int64_t)1 << nlev) + 1;
+    for (int64_t e = gw; e < cnt; e += warps) {
+        const uint32_t i = a.lc_idx[e];
+        const uint32_t s = a.perm[i];
+        const double r_in = a.r_src[s], v_in = a.v_src[s], ell = a.l_src[s];
+        const double gn = gnum_of<true>(i, a.n, a.G, a.M, Mpt);
         int lvmax = 0;
         double ro = r_in, vo = v_in;
         if (!(r_in < 1.0e-30)) {
-            double l2 = dmul(ell, ell);
+            const double l2 = dmul(ell, ell);
             double rho = sqrt(r_in);
             double v = v_in, t = 0.0;
-            double dtau;
+            double hg;
             if (r_in > 1.0e-30 && a.N_taumin > 0)
-                dtau = ddiv(a.dt, dmul(dmul(2.0, r_in), (double)a.N_taumin));
+                hg = __ddiv_rn(a.dt, dmul(dmul(2.0, r_in), (double)a.N_taumin));
             else
-                dtau = ddiv(a.dt, 100.0);
+                hg = __ddiv_rn(a.dt, 100.0);
+            const double dtau = my_sub ? __ddiv_rn(hg, (double)my_sub) : 0.0;
+            const double hdt = dmul(0.5, dtau);
             int64_t steps = 0;
             bool done = false;
             for (;;) {
                 if (t >= a.dt) break;
-                double rn, vn, tn;
-                int lv = tau_step_lc(rho, v, t, dtau, a.tol_r, a.tol_v, a.nlev, gn, l2,
-                                     a.out_type, rn, vn, tn);
-                if (lv < 0) lvmax = -1;
-                else if (lvmax >= 0 && lv > lvmax) lvmax = lv;
+                // ---- one adaptive tau-step from (rho, v, t) over hg
+                double pr = rho, pv = v, pt = t, pf = acc_lc<true>(rho, gn, l2);
+                double rn = rho, vn = v, tn = t;
+                int acc_lv = -2;               // accepted level (-1: fallback)
+                int kcheck = 0;
+                int64_t next_end = 5;          // substeps after which level kcheck's fine pass ends
+                for (int64_t ss = 0; acc_lv == -2; ss++) {
+                    if (ss < my_sub) {
+                        const double vh = dadd(pv, dmul(hdt, pf));
+                        const double rnx = dadd(pr, dmul(dtau, dmul(dmul(0.5, pr), vh)));
+                        const double f2 = acc_lc<true>(rnx, gn, l2);
+                        const double vnx = dadd(vh, dmul(hdt, f2));
+                        const double rm = dmul(0.5, dadd(pr, rnx));
+                        pt = dadd(pt, dmul(dtau, dmul(rm, rm)));
+                        pr = rnx;
+                        pv = vnx;
+                        pf = f2;
+                    }
+                    if (kcheck < nlev && ss + 1 == next_end) {
+                        const int lf = 1 + kcheck, lcz = kcheck;  // fine(k) lane, coarse(k) lane
+                        const double rF = __shfl_sync(0xffffffffu, pr, lf);
+                        const double vF = __shfl_sync(0xffffffffu, pv, lf);
+                        const double tF = __shfl_sync(0xffffffffu, pt, lf);
+                        const double rC = __shfl_sync(0xffffffffu, pr, lcz);
+                        const double vC = __shfl_sync(0xffffffffu, pv, lcz);
+                        const double tC = __shfl_sync(0xffffffffu, pt, lcz);
+                        const double rsq = dmul(rF, rF);
+                        if (converged<true>(rC, vC, rF, vF, rsq, a.tol_r, a.tol_v)) {
+                            if (a.out_type == 0) { rn = rC; vn = vC; tn = tC; }
+                            else if (a.out_type == 1) { rn = rF; vn = vF; tn = tF; }
+                            else {
+                                double rr = dsub(dmul(4.0, rF), dmul(3.0, rC));
+                                vn = dsub(dmul(4.0, vF), dmul(3.0, vC));
+                                tn = dsub(dmul(4.0, tF), dmul(3.0, tC));
+                                if (rr < 0.0) rr = 0.0;
+                                rn = rr;
+                            }
+                            acc_lv = kcheck;
+                        } else if (!(isfinite(rF) && isfinite(vF))) {
+                            rn = rF; vn = vF; tn = tF;  // non-finite: stop climbing
+                            acc_lv = -1;
+                        }
+                        kcheck++;
+                        next_end = 4 * ((int64_t)1 << kcheck) + 1;
+                    }
+                    if (acc_lv == -2 && kcheck >= nlev && ss + 1 == fb_sub) {
+                        rn = __shfl_sync(0xffffffffu, pr, nlev + 1);
+                        vn = __shfl_sync(0xffffffffu, pv, nlev + 1);
+                        tn = __shfl_sync(0xffffffffu, pt, nlev + 1);
+                        acc_lv = -1;
+                    }
+                }
+                if (acc_lv < 0) lvmax = -1;
+                else if (lvmax >= 0 && acc_lv > lvmax) lvmax = acc_lv;
+                // ---- physical-time bookkeeping of nsphere.c:2290-2323
                 if (tn > a.dt) {
                     double alpha = 0.0;
-                    if (fabs(dsub(tn, t)) > 1.0e-30) alpha = ddiv(dsub(a.dt, t), dsub(tn, t));
-                    double rf = dadd(rho, dmul(alpha, dsub(rn, rho)));
-                    double vf = dadd(v, dmul(alpha, dsub(vn, v)));
+                    if (fabs(dsub(tn, t)) > 1.0e-30) alpha = __ddiv_rn(dsub(a.dt, t), dsub(tn, t));
+                    const double rf = dadd(rho, dmul(alpha, dsub(rn, rho)));
+                    const double vf = dadd(v, dmul(alpha, dsub(vn, v)));
                     ro = dmul(rf, rf);
                     vo = vf;
                     done = true;
@@ -307,28 +378,30 @@ __global__ void __launch_bounds__(128) k_levi_civita(StepArgs a)
                 rho = rn; v = vn; t = tn;
                 steps++;
                 if (steps > a.max_tau_steps || !(isfinite(rho) && isfinite(t))) {
-                    atomicOr(&a.ctr->status, NSG_ST_TAU_CAP);
+                    if (lane == 0) atomicOr(&a.ctr->status, NSG_ST_TAU_CAP);
                     break;
                 }
             }
             if (!done) { ro = dmul(rho, rho); vo = v; }
         }
-        a.r_out[i] = ro;
-        a.v_out[i] = vo;
-        a.level[i] = (int8_t)(lvmax < 0 ? kLevelLcFallback : kLevelLcBase + lvmax);
+        if (lane == 0) {
+            a.r_out[i] = ro;
+            a.v_out[i] = vo;
+            a.level[i] = (int8_t)(lvmax < 0 ? kLevelLcFallback : kLevelLcBase + lvmax);
+        }
     }
 }
 
 // ------------------------------------------------------------ fixed-step KDK
 
 // First half of the method-2 body (nsphere.c:5487-5505): kick with the rank of the
-// current order, then drift.
+// current order, then drift.  a0 is gnum_i/r^2 + ell^2/r^3 at the current radius
+// and rank: the force the reference recomputes for this kick (same operands,
+// same result).
 __global__ void __launch_bounds__(256)
 k_kick_drift(double *__restrict__ r, double *__restrict__ v, const double *__restrict__ a0,
              int64_t n, double dt)
 {
-    // a0 is gnum_i/r^2 + ell^2/r^3 at the current radius and rank: the force the
-    // reference recomputes for this kick (same operands, same result).
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         double vi = dadd(v[i], dmul(dmul(0.5, a0[i]), dt));
@@ -341,10 +414,9 @@ static StepArgs make_args(nsg_ctx *c)
 {
     // the fused pass reads copy `src` through c->perm and writes copy `dst`
     StepArgs a{};
-    const int src = c->cur, s = 1 - c->cur;
-    a.r_in = c->r[s]; a.v_in = c->vr[s]; a.ell = c->ell[s]; a.a0 = c->a0;
-    a.r_out = c->r[s]; a.v_out = c->vr[s];
-    a.ell_out = c->ell[s]; a.aux_out = c->aux[s]; a.id_out = c->id[s]; a.inv = c->inv;
+    const int src = c->cur, dst = 1 - c->cur;
+    a.r_out = c->r[dst]; a.v_out = c->vr[dst]; a.ell_out = c->ell[dst]; a.aux_out = c->aux[dst];
+    a.id_out = c->id[dst]; a.inv = c->inv; a.a0 = c->a0; a.split = c->split;
     a.perm = c->perm;
     a.r_src = c->r[src]; a.v_src = c->vr[src]; a.l_src = c->ell[src]; a.aux_src = c->aux[src];
     a.id_src = c->id[src];
@@ -352,7 +424,6 @@ static StepArgs make_args(nsg_ctx *c)
     a.n = c->n;
     a.G = c->p.G; a.M = c->p.M_total; a.dt = c->p.dt;
     a.tol_r = c->p.tol_r; a.tol_v = c->p.tol_v;
-    a.max_subdiv = c->p.max_subdiv;
     int nlev = 0;
     for (int64_t N = 1; N <= c->p.max_subdiv && nlev < kMaxLevels - 1; N *= 2) nlev++;
     a.nlev = nlev;
@@ -372,7 +443,7 @@ static StepArgs make_args(nsg_ctx *c)
     a.N_taumin = c->p.N_taumin;
     a.max_tau_steps = c->p.max_tau_steps;
     a.ctr = c->ctr;
-    for (int b = 0; b < 2; b++) { a.q_idx[b] = c->q_idx[b]; a.q_r[b] = c->q_r[b]; a.q_v[b] = c->q_v[b]; }
+    a.q_idx = c->q_idx[0]; a.q_r = c->q_r[0]; a.q_v = c->q_v[0];
     a.lc_idx = c->lc_idx;
     return a;
 }
@@ -386,37 +457,43 @@ int integrate_adaptive(nsg_ctx *c)
     // reset queue counters (qcount[] and lc_count live at the head of DevCounters)
     e = cudaMemsetAsync(&c->ctr->lc_count, 0, sizeof(unsigned) * (kMaxLevels + 2), s);
     if (e != cudaSuccess) return cuda_err(c, e, "memset queue counters");
-    const int grid = grid_for(c, c->n, 256, 8);
-    {
-        // algorithmic bytes: perm 4, gather r v ell id 28, write r v ell id 28, inv 4, level 1
-        ProfScope ps(c, "gather_level0", (double)c->n * (4 + 28 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)));
-        if (c->p.carry_aux) k_gather_level0<true><<<grid, 256, 0, s>>>(a);
-        else k_gather_level0<false><<<grid, 256, 0, s>>>(a);
-        c->launches += 1;
-    }
-    c->cur = 1 - c->cur;
-    c->inv_valid = true;
-    c->sorted = false;  // radii moved
-    if (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF) {
+    const bool lc = (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF);
+    if (lc) {
+        // Levi-Civita particles start on the side stream as soon as the order is known
         e = cudaEventRecord(c->ev_fork, s);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
         if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
-        k_levi_civita<<<c->num_sms * 4, 128, 0, c->side>>>(a);
-        c->launches += 1;
+        k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, c->side>>>(a);
+        k_levi_civita_lanes<<<c->num_sms * 4, 128, 0, c->side>>>(a);
+        c->launches += 2;
         e = cudaEventRecord(c->ev_join, c->side);
         if (e != cudaSuccess) return cuda_err(c, e, "join record");
     }
     {
-        ProfScope ps(c, "leap_levels", 0.0);
-        for (int k = 1; k < a.nlev; k++) k_level<<<c->num_sms * 8, 256, 0, s>>>(a, k);
-        c->launches += a.nlev - 1;
+        // algorithmic bytes: perm 4, gather r v ell id 28, write r v ell id 28, inv 4, level 1
+        ProfScope ps(c, "gather_level0", (double)c->n * (4 + 28 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)));
+        const int grid = grid_for(c, c->n, 256, 8);
+        if (c->p.carry_aux) k_gather_level0<true><<<grid, 256, 0, s>>>(a);
+        else k_gather_level0<false><<<grid, 256, 0, s>>>(a);
+        c->launches += 1;
     }
-    if (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF) {
+    if (a.nlev > 1) {
+        ProfScope ps(c, "leap_levels", 0.0);
+        int G = 1;
+        while (G < a.nlev - 1) G <<= 1;
+        k_levels_lanes<<<c->num_sms * 4, 256, 0, s>>>(a, G);
+        c->launches += 1;
+    }
+    if (lc) {
         e = cudaStreamWaitEvent(s, c->ev_join, 0);
         if (e != cudaSuccess) return cuda_err(c, e, "join wait");
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(c, e, "integrator kernels");
+    c->cur = 1 - c->cur;
+    c->inv_valid = true;
+    c->sorted = false;  // radii moved
+    c->split_valid = true;
     return NSG_OK;
 }
 

@@ -21,6 +21,8 @@ constexpr int kRadixThreads = 256;
 constexpr int kRadixItems = 16;       // keys per thread per tile
 constexpr int kRadixTile = kRadixThreads * kRadixItems;
 constexpr int kReduceBlocks = 1024;   // fixed block count of energy partial sums
+constexpr int kBucketTarget = 2048;   // near-sorted sort: sorted positions per splitter (power of 2)
+constexpr int kBucketCap = 6144;      // entries one bucket block sorts (512 threads x 12)
 
 // Device-resident counters and flags of one context (a single allocation).
 struct DevCounters {
@@ -30,7 +32,7 @@ struct DevCounters {
     unsigned long long level_hist[kStatBins];
     double energy[2];                       // K, W of the last sort
     double point_mass;                      // current central point mass
-    unsigned int bucket_overflow;           // near-sorted sort overflow flag
+    unsigned int need_fallback;             // 1: the radix sort must run this sort
     unsigned int pad;
 };
 
@@ -76,6 +78,12 @@ struct nsg_ctx {
     uint32_t *digit_tot = nullptr;   // [256]
     uint32_t *perm = nullptr;        // result of sort_perm: source index per sorted position
 
+    // near-sorted bucket sort (nsg_bucket.cu)
+    uint64_t *split = nullptr;       // [nb] splitter keys from the last sort
+    bool split_valid = false;
+    unsigned int *bcnt = nullptr, *boff = nullptr;  // [nb]
+    uint64_t *bkey = nullptr, *bpay = nullptr;      // [nb * kBucketCap]
+
     // leapfrog level queues (ping-pong) and the Levi-Civita list
     uint32_t *q_idx[2] = {nullptr, nullptr};
     double *q_r[2] = {nullptr, nullptr}, *q_v[2] = {nullptr, nullptr};
@@ -102,30 +110,38 @@ namespace nsg {
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-// Division runs on the integer/FP32 pipes (nsg_div.cuh), bit-identical to IEEE.
+// Division: throughput-bound kernels divide on the integer/FP32 pipes
+// (div_rn, nsg_div.cuh); latency-bound ones (a few long serial chains) use the
+// FP64 pipe's shorter dependent sequence.  Both are IEEE round-to-nearest, so
+// the choice never changes a result bit.
+template <bool HW>
+__device__ __forceinline__ double ddivx(double a, double b) { return HW ? __ddiv_rn(a, b) : div_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return div_rn(a, b); }
 
 // -(G) * (i / n) * M (+ the point-mass term when present), nsphere.c:513.
+template <bool HW = false>
 __device__ __forceinline__ double gnum_of(int64_t i, int64_t n, double G, double M, double Mpt)
 {
-    double g = dmul(dmul(-G, ddiv((double)i, (double)n)), M);
+    double g = dmul(dmul(-G, ddivx<HW>((double)i, (double)n)), M);
     if (Mpt != 0.0) g = dsub(g, dmul(G, Mpt));
     return g;
 }
 
 // gravity + centrifugal: gnum/(r*r) + l2/(r*r*r), nsphere.c:502-535.
+template <bool HW = false>
 __device__ __forceinline__ double acc_leap(double r, double gnum, double l2)
 {
     double r2 = dmul(r, r);
-    return dadd(ddiv(gnum, r2), ddiv(l2, dmul(r2, r)));
+    return dadd(ddivx<HW>(gnum, r2), ddivx<HW>(l2, dmul(r2, r)));
 }
 
 // Levi-Civita: gnum/(rho*rho) + l2/(rho*rho*rho*rho), nsphere.c:563-599, 1777-1787.
+template <bool HW = false>
 __device__ __forceinline__ double acc_lc(double rho, double gnum, double l2)
 {
     double p2 = dmul(rho, rho);
     double p4 = dmul(dmul(p2, rho), rho);
-    return dadd(ddiv(gnum, p2), ddiv(l2, p4));
+    return dadd(ddivx<HW>(gnum, p2), ddivx<HW>(l2, p4));
 }
 
 // Order-preserving map of a double to uint64: -0.0 -> +0.0, NaN -> all ones.
@@ -134,6 +150,13 @@ __device__ __forceinline__ uint64_t radius_key(double r)
     if (r != r) return ~0ull;
     unsigned long long u = (r == 0.0) ? 0ull : (unsigned long long)__double_as_longlong(r);
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// Splitter of the next near-sorted sort: key(r) at sorted positions b*kBucketTarget,
+// written by the passes that consume a sort (from the sorted start-of-step radii).
+__device__ __forceinline__ void write_splitter(uint64_t *S, int64_t i, double r)
+{
+    if ((i & (kBucketTarget - 1)) == 0) S[i / kBucketTarget] = (i == 0) ? 0ull : radius_key(r);
 }
 
 __device__ __forceinline__ unsigned lanemask_lt()
@@ -180,6 +203,8 @@ int sort_state_kick(nsg_ctx *c);                      // same, plus the second h
 int integrate_adaptive(nsg_ctx *c);                   // method 3 / 5: sort_perm, then fused gather + levels
 int kdk_first_half(nsg_ctx *c);                       // kick (a0 of the current rank) + drift
 int compute_energy(nsg_ctx *c);                       // K, W of the sorted live copy
+int bucket_sort_perm(nsg_ctx *c);                     // near-sorted fast path (sets need_fallback)
+int bucket_setup(nsg_ctx *c);
 int launch_gather(nsg_ctx *c, const int32_t *d_ids, int k, double *d_out, int32_t *d_rank);
 int launch_level_hist(nsg_ctx *c);
 int launch_ids_from_double(nsg_ctx *c, const double *d_src, int32_t *d_dst, int64_t n);

@@ -23,6 +23,7 @@ __global__ void k_seed_keys(const double *__restrict__ r, const int32_t *__restr
                             int64_t n, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
                             DevCounters *ctr)
 {
+    if (!ctr->need_fallback) return;
     bool nan_seen = false;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
@@ -38,8 +39,9 @@ __global__ void k_seed_keys(const double *__restrict__ r, const int32_t *__restr
 // Per-tile histogram of one digit.  counts is digit-major: counts[d * ntiles + t].
 __global__ void __launch_bounds__(kRadixThreads)
 k_tile_hist(const uint64_t *__restrict__ keys, int64_t n, int shift, int ntiles,
-            uint32_t *__restrict__ counts)
+            uint32_t *__restrict__ counts, const DevCounters *__restrict__ ctr)
 {
+    if (!ctr->need_fallback) return;
     __shared__ uint32_t h[kRadixBuckets];
     for (int d = threadIdx.x; d < kRadixBuckets; d += blockDim.x) h[d] = 0;
     __syncthreads();
@@ -86,8 +88,10 @@ __device__ __forceinline__ uint32_t block_excl_scan_1024(uint32_t v, uint32_t *w
 
 // Sum of each digit's row of tile counts.  One block per digit.
 __global__ void __launch_bounds__(1024)
-k_digit_totals(const uint32_t *__restrict__ counts, int ntiles, uint32_t *__restrict__ tot)
+k_digit_totals(const uint32_t *__restrict__ counts, int ntiles, uint32_t *__restrict__ tot,
+               const DevCounters *__restrict__ ctr)
 {
+    if (!ctr->need_fallback) return;
     __shared__ uint32_t wsum[32];
     const uint32_t *row = counts + (int64_t)blockIdx.x * ntiles;
     uint32_t s = 0;
@@ -107,8 +111,10 @@ k_digit_totals(const uint32_t *__restrict__ counts, int ntiles, uint32_t *__rest
 // Turns each digit's row into global exclusive offsets: base(digit) + prefix over
 // tiles.  One block per digit.
 __global__ void __launch_bounds__(1024)
-k_digit_scan(uint32_t *__restrict__ counts, int ntiles, const uint32_t *__restrict__ tot)
+k_digit_scan(uint32_t *__restrict__ counts, int ntiles, const uint32_t *__restrict__ tot,
+             const DevCounters *__restrict__ ctr)
 {
+    if (!ctr->need_fallback) return;
     __shared__ uint32_t warp_tot[32];
     __shared__ uint32_t total;
     __shared__ uint32_t base_s;
@@ -136,8 +142,10 @@ k_digit_scan(uint32_t *__restrict__ counts, int ntiles, const uint32_t *__restri
 __global__ void __launch_bounds__(kRadixThreads)
 k_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
           uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n,
-          int shift, int ntiles, const uint32_t *__restrict__ offsets)
+          int shift, int ntiles, const uint32_t *__restrict__ offsets,
+          const DevCounters *__restrict__ ctr)
 {
+    if (!ctr->need_fallback) return;
     constexpr int W = kRadixThreads / 32;
     __shared__ uint32_t whist[W][kRadixBuckets];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -204,7 +212,7 @@ k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
                     const double *__restrict__ x0,
                     double *__restrict__ r1, double *__restrict__ v1, double *__restrict__ l1,
                     int32_t *__restrict__ id1, double *__restrict__ x1,
-                    double *__restrict__ a0, int32_t *__restrict__ inv,
+                    double *__restrict__ a0, int32_t *__restrict__ inv, uint64_t *__restrict__ split,
                     double G, double M, double dt, const DevCounters *__restrict__ ctr)
 {
     const double Mpt = ctr->point_mass;
@@ -223,6 +231,7 @@ k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
         if (AUX) x1[p] = x0[s];
         inv[idv] = (int32_t)p;
         a0[p] = acc;
+        write_splitter(split, p, r);
     }
 }
 
@@ -286,6 +295,15 @@ int sort_perm(nsg_ctx *c)
     const int src = c->cur;
     const int ntiles = (int)((n + kRadixTile - 1) / kRadixTile);
     cudaStream_t s = c->stream;
+    // near-sorted fast path when the array is in the order of a previous sort;
+    // the radix kernels below run only if it overflowed (or it was not used)
+    if (c->split_valid && c->p.sort_mode == 0) {
+        if (int rc = bucket_sort_perm(c)) return rc;
+    } else {
+        // any non-zero value selects the radix path (bytes set to 0x01)
+        cudaError_t e = cudaMemsetAsync(&c->ctr->need_fallback, 1, sizeof(unsigned), s);
+        if (e != cudaSuccess) return cuda_err(c, e, "fallback flag");
+    }
     {
         ProfScope ps(c, "sort_seed", (double)n * (8 + 4 + 8 + 4));
         k_seed_keys<<<grid_for(c, n, 256), 256, 0, s>>>(c->r[src], c->id[src], n, c->keys[0],
@@ -296,12 +314,13 @@ int sort_perm(nsg_ctx *c)
         ProfScope ps(c, "sort_radix", (double)n * 8 * (8 + 12 + 12));
         for (int pass = 0; pass < 8; pass++) {
             int shift = pass * kRadixBits;
-            k_tile_hist<<<ntiles, kRadixThreads, 0, s>>>(c->keys[kb], n, shift, ntiles, c->tile_counts);
-            k_digit_totals<<<kRadixBuckets, 1024, 0, s>>>(c->tile_counts, ntiles, c->digit_tot);
-            k_digit_scan<<<kRadixBuckets, 1024, 0, s>>>(c->tile_counts, ntiles, c->digit_tot);
+            k_tile_hist<<<ntiles, kRadixThreads, 0, s>>>(c->keys[kb], n, shift, ntiles, c->tile_counts,
+                                                         c->ctr);
+            k_digit_totals<<<kRadixBuckets, 1024, 0, s>>>(c->tile_counts, ntiles, c->digit_tot, c->ctr);
+            k_digit_scan<<<kRadixBuckets, 1024, 0, s>>>(c->tile_counts, ntiles, c->digit_tot, c->ctr);
             k_scatter<<<ntiles, kRadixThreads, 0, s>>>(c->keys[kb], c->vals[kb], c->keys[1 - kb],
                                                        c->vals[1 - kb], n, shift, ntiles,
-                                                       c->tile_counts);
+                                                       c->tile_counts, c->ctr);
             kb = 1 - kb;
         }
     }
@@ -322,8 +341,8 @@ static int gather(nsg_ctx *c, bool kick)
 #define NSG_GATHER(AUXV, KICKV)                                                                   \
     k_gather_rank_force<AUXV, KICKV><<<grid, 256, 0, s>>>(                                        \
         c->perm, n, c->r[src], c->vr[src], c->ell[src], c->id[src], c->aux[src], c->r[dst],      \
-        c->vr[dst], c->ell[dst], c->id[dst], c->aux[dst], c->a0, c->inv, c->p.G, c->p.M_total,   \
-        c->p.dt, c->ctr)
+        c->vr[dst], c->ell[dst], c->id[dst], c->aux[dst], c->a0, c->inv, c->split, c->p.G,       \
+        c->p.M_total, c->p.dt, c->ctr)
     if (c->p.carry_aux) { if (kick) NSG_GATHER(true, true); else NSG_GATHER(true, false); }
     else { if (kick) NSG_GATHER(false, true); else NSG_GATHER(false, false); }
 #undef NSG_GATHER
@@ -333,6 +352,7 @@ static int gather(nsg_ctx *c, bool kick)
     c->cur = dst;
     c->sorted = true;
     c->inv_valid = true;
+    c->split_valid = true;
     return NSG_OK;
 }
 

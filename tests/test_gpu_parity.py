@@ -265,3 +265,42 @@ def test_integer_pipe_division_matches_ieee(nsg):
         assert mism == 0, "first mismatch a=%r b=%r" % first
         total += fast
     assert total > 0.5 * 600_000_000  # most pairs take the integer path
+
+
+@pytest.mark.parametrize("ntie", [100, 30000])
+def test_near_sorted_sort_ties_and_overflow(nsg, oracle, ntie):
+    """Second sort of a state runs the near-sorted bucket path: equal radii are
+    ordered by id inside a bucket; a tie run larger than a bucket overflows it and
+    the radix sort takes over."""
+    rng = np.random.default_rng(ntie)
+    n = 120_000
+    r = rng.uniform(0.0, 2.0, n)
+    r[rng.choice(n, ntie, replace=False)] = 1.0
+    ids = rng.permutation(n).astype(np.int32)
+    z = rng.normal(size=n)
+    with _ctx(nsg) as c:
+        c.upload(r, z, z, ids)
+        c.sort()
+        c.clear_status()
+        c.sort()
+        gr, gv, _, gid = c.download()
+        st = c.status()
+    orr, ov, _, oid = oracle.sort(r, z, z, ids)
+    assert np.array_equal(gid, oid) and np.array_equal(gr, orr) and np.array_equal(gv, ov)
+    assert bool(st & nsg.ST_SORT_FALLBACK) == (ntie > 6144)
+
+
+def test_near_sorted_sort_after_moves(nsg, oracle):
+    """Sorts after each of 30 KDK steps with a large dt (many rank crossings) use
+    the bucket path and stay bit-exact."""
+    n = 50_000
+    r0, v0, l0, i0 = ics.plummer(n, seed=8)
+    p = oracle.params(dt=2e-2)
+    cur = (r0, v0, l0, i0)
+    for _ in range(30):
+        cur = oracle.step_kdk(p, *cur)
+    with _ctx(nsg, dt=2e-2, method=nsg.METHOD_KDK) as c:
+        c.upload(r0, v0, l0, i0)
+        c.step(30)
+        r, vr, ell, ids = c.download()
+    assert np.array_equal(ids, cur[3]) and np.array_equal(r, cur[0]) and np.array_equal(vr, cur[1])

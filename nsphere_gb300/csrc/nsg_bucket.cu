@@ -25,7 +25,7 @@ namespace nsg {
 constexpr int kBucketThreads = 512;
 constexpr int kBucketItems = 12;
 constexpr int kBucketWarps = kBucketThreads / 32;
-constexpr int kSeg = kBucketItems * 32;      // positions owned by one warp
+
 
 // Largest b with S[b] <= key (S[0] is the smallest key), searched from home.
 __device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int nb, uint64_t key, int home)
@@ -132,28 +132,33 @@ k_bucket_scan(const unsigned int *__restrict__ cnt, int nb, int cap, unsigned in
     }
 }
 
-// One stable LSD pass on 8 bits of the key chosen by `digit_of`, over the block's
-// items held in registers (warp w owns positions [w*kSeg, (w+1)*kSeg), item j of
-// lane l is position w*kSeg + j*32 + l).  Items are exchanged through shared memory.
+// One stable LSD pass on 8 bits chosen by `digit_of`, over the block's items held
+// in registers.  Warp w owns positions [w*S, (w+1)*S) with S = J*32: item j < J of
+// lane l is position w*S + j*32 + l, so walking j and then lanes visits positions
+// in order and the match.any ranks are stable.  J = ceil(count / 512) adapts the
+// work to the bucket's fill; items are exchanged through shared memory.
 template <typename DigitFn>
 __device__ __forceinline__ void block_radix_pass(uint64_t (&k)[kBucketItems], uint64_t (&v)[kBucketItems],
-                                                 DigitFn digit_of, uint32_t (*whist)[256],
+                                                 int J, DigitFn digit_of, uint32_t (*whist)[256],
                                                  uint32_t *dtot, uint64_t *xk)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int S = J * 32;
     const unsigned lt = lanemask_lt();
     for (int d = threadIdx.x; d < kBucketWarps * 256; d += blockDim.x) (&whist[0][0])[d] = 0;
     __syncthreads();
     uint32_t rd[kBucketItems];   // (rank within warp and digit) << 8 | digit
 #pragma unroll
     for (int j = 0; j < kBucketItems; j++) {
-        unsigned d = digit_of(k[j], v[j]);
-        unsigned peers = __match_any_sync(0xffffffffu, d);
-        uint32_t c = whist[w][d];
-        rd[j] = ((c + __popc(peers & lt)) << 8) | d;
-        __syncwarp();
-        if (lane == __ffs(peers) - 1) whist[w][d] = c + __popc(peers);
-        __syncwarp();
+        if (j < J) {
+            unsigned d = digit_of(k[j], v[j]);
+            unsigned peers = __match_any_sync(0xffffffffu, d);
+            uint32_t c = whist[w][d];
+            rd[j] = ((c + __popc(peers & lt)) << 8) | d;
+            __syncwarp();
+            if (lane == __ffs(peers) - 1) whist[w][d] = c + __popc(peers);
+            __syncwarp();
+        }
     }
     __syncthreads();
     // digit-major exclusive offsets: per digit over warps, then over digits
@@ -187,23 +192,27 @@ __device__ __forceinline__ void block_radix_pass(uint64_t (&k)[kBucketItems], ui
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < kBucketItems; j++) {
-        const uint32_t d = rd[j] & 255u;
-        uint32_t pos = dtot[d] + whist[w][d] + (rd[j] >> 8);
-        xk[pos] = k[j];
+        if (j < J) {
+            const uint32_t d = rd[j] & 255u;
+            xk[dtot[d] + whist[w][d] + (rd[j] >> 8)] = k[j];
+        }
     }
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < kBucketItems; j++) k[j] = xk[w * kSeg + j * 32 + lane];
+    for (int j = 0; j < kBucketItems; j++)
+        if (j < J) k[j] = xk[w * S + j * 32 + lane];
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < kBucketItems; j++) {
-        const uint32_t d = rd[j] & 255u;
-        uint32_t pos = dtot[d] + whist[w][d] + (rd[j] >> 8);
-        xk[pos] = v[j];
+        if (j < J) {
+            const uint32_t d = rd[j] & 255u;
+            xk[dtot[d] + whist[w][d] + (rd[j] >> 8)] = v[j];
+        }
     }
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < kBucketItems; j++) v[j] = xk[w * kSeg + j * 32 + lane];
+    for (int j = 0; j < kBucketItems; j++)
+        if (j < J) v[j] = xk[w * S + j * 32 + lane];
     __syncthreads();
 }
 
@@ -240,38 +249,40 @@ k_bucket_sort(const unsigned int *__restrict__ cnt, const unsigned int *__restri
 
     const int b = blockIdx.x;
     const uint32_t m = cnt[b];
+    if (m == 0) return;
     const uint32_t base = off[b];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int J = (int)((m + kBucketThreads - 1) / kBucketThreads);   // 1 .. kBucketItems
+    const int S = J * 32;
     const int64_t src0 = (int64_t)b * cap;
     uint64_t k[kBucketItems], v[kBucketItems];
     uint64_t kmin = ~0ull, kmax = 0ull;
 #pragma unroll
     for (int j = 0; j < kBucketItems; j++) {
-        uint32_t pos = w * kSeg + j * 32 + lane;
-        bool ok = pos < m;
+        const uint32_t pos = w * S + j * 32 + lane;
+        const bool ok = (j < J) && pos < m;
         k[j] = ok ? bkey[src0 + pos] : ~0ull;
         v[j] = ok ? bpay[src0 + pos] : ~0ull;
         if (ok) { kmin = k[j] < kmin ? k[j] : kmin; kmax = k[j] > kmax ? k[j] : kmax; }
     }
-    if (m == 0) return;
     kmin = block_reduce_u64(kmin, true, red);
     kmax = block_reduce_u64(kmax, false, red);
     const uint64_t diff = kmin ^ kmax;
     const int kbits = diff ? 64 - __clzll((long long)diff) : 0;
     for (int shift = 0; shift < kbits; shift += 8)
-        block_radix_pass(k, v, [shift](uint64_t kk, uint64_t) { return (unsigned)(kk >> shift) & 255u; },
+        block_radix_pass(k, v, J, [shift](uint64_t kk, uint64_t) { return (unsigned)(kk >> shift) & 255u; },
                          whist, dtot, xk);
     // ties on the key (equal radii) are ordered by id: re-sort by id, then by key
     int tie = 0;
     {
-        // after the passes item (w, j, lane) sits at position w*kSeg + j*32 + lane
 #pragma unroll
-        for (int j = 0; j < kBucketItems; j++) xk[w * kSeg + j * 32 + lane] = k[j];
+        for (int j = 0; j < kBucketItems; j++)
+            if (j < J) xk[w * S + j * 32 + lane] = k[j];
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < kBucketItems; j++) {
-            uint32_t pos = w * kSeg + j * 32 + lane;
-            if (pos + 1 < m && xk[pos] == xk[pos + 1]) tie = 1;
+            const uint32_t pos = w * S + j * 32 + lane;
+            if (j < J && pos + 1 < m && xk[pos] == xk[pos + 1]) tie = 1;
         }
         tie = __syncthreads_or(tie);
     }
@@ -279,24 +290,28 @@ k_bucket_sort(const unsigned int *__restrict__ cnt, const unsigned int *__restri
         uint64_t imin = ~0ull, imax = 0ull;
 #pragma unroll
         for (int j = 0; j < kBucketItems; j++) {
-            uint32_t pos = w * kSeg + j * 32 + lane;
-            if (pos < m) { uint64_t x = v[j] >> 32; imin = x < imin ? x : imin; imax = x > imax ? x : imax; }
+            const uint32_t pos = w * S + j * 32 + lane;
+            if (j < J && pos < m) {
+                const uint64_t x = v[j] >> 32;
+                imin = x < imin ? x : imin;
+                imax = x > imax ? x : imax;
+            }
         }
         imin = block_reduce_u64(imin, true, red);
         imax = block_reduce_u64(imax, false, red);
         const uint64_t idiff = imin ^ imax;
         const int ibits = idiff ? 64 - __clzll((long long)idiff) : 0;
         for (int shift = 0; shift < ibits; shift += 8)
-            block_radix_pass(k, v, [shift](uint64_t, uint64_t vv) { return (unsigned)((vv >> 32) >> shift) & 255u; },
+            block_radix_pass(k, v, J, [shift](uint64_t, uint64_t vv) { return (unsigned)((vv >> 32) >> shift) & 255u; },
                              whist, dtot, xk);
         for (int shift = 0; shift < kbits; shift += 8)
-            block_radix_pass(k, v, [shift](uint64_t kk, uint64_t) { return (unsigned)(kk >> shift) & 255u; },
+            block_radix_pass(k, v, J, [shift](uint64_t kk, uint64_t) { return (unsigned)(kk >> shift) & 255u; },
                              whist, dtot, xk);
     }
 #pragma unroll
     for (int j = 0; j < kBucketItems; j++) {
-        uint32_t pos = w * kSeg + j * 32 + lane;
-        if (pos < m) perm[base + pos] = (uint32_t)(v[j] & 0xffffffffu);
+        const uint32_t pos = w * S + j * 32 + lane;
+        if (j < J && pos < m) perm[base + pos] = (uint32_t)(v[j] & 0xffffffffu);
     }
 }
 

@@ -273,8 +273,9 @@ __global__ void __launch_bounds__(256) k_lc_select(StepArgs a)
 // adaptive tau-step (nsphere.c:2077-2186): lane 0 the coarse N=1 pass (3
 // substeps), lane 1+k the fine pass of level k (4*2^k+1 substeps; it is also the
 // coarse pass of level k+1), lane nlev+1 the fallback fine pass at N = 2^nlev.
-// Requires nlev + 2 <= 32 (max_subdiv < 2^30, checked by the host).
-__global__ void __launch_bounds__(128) k_levi_civita_lanes(StepArgs a)
+// Requires nlev + 2 <= 32 (max_subdiv < 2^30, checked by the host).  Launched
+// with one warp per block.
+__global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
 {
     const unsigned cnt = a.ctr->lc_count;
     if (cnt == 0) return;
@@ -464,7 +465,10 @@ int integrate_adaptive(nsg_ctx *c)
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
         if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
         k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, c->side>>>(a);
-        k_levi_civita_lanes<<<c->num_sms * 4, 128, 0, c->side>>>(a);
+        // one warp per block, so consecutive particles land on different SMs: a
+        // warp-wide FP64 instruction occupies an SM's FP64 pipe for many cycles,
+        // and these chains are latency-bound
+        k_levi_civita_lanes<<<c->num_sms * 4, 32, 0, c->side>>>(a);
         c->launches += 2;
         e = cudaEventRecord(c->ev_join, c->side);
         if (e != cudaSuccess) return cuda_err(c, e, "join record");

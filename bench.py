@@ -12,11 +12,12 @@ the 129 MB L2, so no flush is needed between steps.
 
 ``--impl reference`` times the reference's own CPU step (its functions built from
 its sources into oracle/_ref; the oracle port when those are absent) on the same
-workload with every host thread, on a bounded sample per step.
+workload with every host thread, one full N-particle step per timed step.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -32,37 +33,44 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s at N=1e7: learned vs plain GPU at equal |ΔE/E|; HBM GB/s"
 UNIT = "particle-steps/s"
-HBM_BYTES_SORT = 72.0       # algorithmic bytes per particle of the sort + rank/force pass
-HBM_BYTES_INTEGRATE = 48.0  # read r, v_r, ell, a0; write r, v_r
+# sort + scan + force pass, algorithmic bytes per particle: read r key 8, gather r v ell id 28,
+# write them 28, write the rank force 8
+SORT_PASS_BYTES = 72.0
+# DRAM bytes per particle of one k_gather_level0 launch (read + write), from an ncu capture
+# of that kernel at N = 5e6 (160.6 MB read + 122.2 MB written per launch)
+GATHER_LEVEL0_TRAFFIC = (160.628224e6 + 122.180864e6) / 5e6
+# IEEE double operations per particle that k_gather_level0 issues at level 0
+# (rank numerator 3, start force 5, coarse pass 9, fine pass 16, test 6, Richardson 6, l^2 1)
+LEVEL0_FLOPS = 46.0
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=10_000_000)
     ap.add_argument("--workload", choices=["adaptive", "kdk"], default="adaptive")
     ap.add_argument("--sched", choices=["plain", "learned"], default="plain")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
 
-def workload(args):
+def workload(args, seed_offset=0):
     from nsphere_gb300 import ics
     if args.workload == "kdk":
-        name = "plummer_kdk_fixed_step"
-        cfg = dict(workload=name, n=args.n, profile="plummer", seed=1, dt=1e-3, method="kdk (reference method 2)")
-        state = ics.plummer(args.n, seed=1)
+        cfg = dict(workload="plummer_kdk_fixed_step", n=args.n, profile="plummer", seed=1 + seed_offset,
+                   dt=1e-3, method="fixed-step leapfrog (reference method 2)")
+        state = ics.plummer(args.n, seed=1 + seed_offset)
         params = dict(dt=1e-3, method=2)
     else:
-        name = "hernquist_adaptive_lc"
-        cfg = dict(workload=name, n=args.n, profile="hernquist a=1 r<=100 isotropic", seed=2, dt=5e-4,
-                   max_levels=8, max_subdiv=128, lc="levi-civita below r=1e-3", tol=1e-7, out_type=2)
-        state = ics.hernquist(args.n, seed=2)
+        cfg = dict(workload="hernquist_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 isotropic",
+                   seed=2 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,
+                   lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
+        state = ics.hernquist(args.n, seed=2 + seed_offset)
         params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
     cfg["l2"] = "inputs larger than L2 (state %.0f MB vs 129 MB L2); no flush" % (args.n * 28 / 1e6)
     cfg["sched"] = args.sched
@@ -104,26 +112,24 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
-        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
+        ok = [r for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
+        sm = [float(r[0]) for r in ok]
+        mx = [float(r[1]) for r in ok if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in self.rows if len(r) >= 7 for k in range(4)
-                          if r[3 + k].lower() == "active"})
+        reasons = sorted({names[k] for r in ok for k in range(4) if r[3 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(sm)}
 
 
-def cpu_baseline(state, params, args, seconds, use_reference=True):
-    """Times the reference CPU step (oracle/_ref, every host thread) on a bounded sample."""
+def cpu_stepper(params):
+    """The reference's own step functions (oracle/_ref, all host threads), else the port."""
     from oracle import build_oracle
     from oracle.oracle import Oracle, Reference
-    r, vr, ell, ids = state
-    kind = "reference"
     try:
-        if not use_reference or not build_oracle.build_reference():
+        if not build_oracle.build_reference():
             raise FileNotFoundError
         R = Reference(fast=True)
-        cores = R.num_threads()
+        cores, kind = R.num_threads(), "reference"
 
         def step(cur):
             if params.get("method") == 2:
@@ -134,10 +140,9 @@ def cpu_baseline(state, params, args, seconds, use_reference=True):
                                         lc_radius=params["lc_radius"], parallel_sort=True)
             return tab[0], tab[1], tab[2], tab[3]
     except (FileNotFoundError, RuntimeError, OSError):
-        kind = "port"
         build_oracle.build_oracle()
         O = Oracle()
-        cores = O.num_threads()
+        cores, kind = O.num_threads(), "port"
         if params.get("method") == 2:
             op = O.params(dt=params["dt"])
 
@@ -149,79 +154,54 @@ def cpu_baseline(state, params, args, seconds, use_reference=True):
 
             def step(cur):
                 return O.step_adaptive(op, *cur)[:4]
-    # bounded sample: whole state while a step fits the budget, else a prefix subsample
+    return step, cores, kind
+
+
+def cpu_baseline(state, params, seconds):
+    """Reference CPU step on the full N-particle state, repeated for about `seconds`."""
+    step, cores, kind = cpu_stepper(params)
+    r, vr, ell, ids = state
     n = len(r)
-    m = n
-    cur = (r[:m], vr[:m], ell[:m], ids[:m].astype(np.float64))
-    t0 = time.perf_counter()
-    cur = step(cur)
-    t1 = time.perf_counter()
-    steps, elapsed = 1, t1 - t0
-    while elapsed < seconds and steps < 1000:
+    cur = (r, vr, ell, ids.astype(np.float64))
+    steps, elapsed = 0, 0.0
+    while (elapsed < seconds or steps == 0) and steps < 1000:
         t0 = time.perf_counter()
         cur = step(cur)
         elapsed += time.perf_counter() - t0
         steps += 1
-    return {"value": m * steps / elapsed, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": "%d steps of the full N=%d state (%.1f s of CPU work, quadsort_parallel, "
-                      "gcc -O2 -ffast-math -fopenmp)" % (steps, m, elapsed)}
+    flags = "gcc -O2 -ffast-math -fopenmp" if kind == "reference" else "gcc -O2 -fopenmp"
+    return {"value": n * steps / elapsed, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": "%d full steps of the N=%d state (%.1f s of CPU work; default quadsort_parallel; %s)"
+                      % (steps, n, elapsed, flags)}
 
 
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return
     cfg, state, params = workload(args)
-    # each step is a bounded sample of the workload: one full step of the N-particle state
-    res = cpu_baseline(state, params, args, seconds=1e-9)
-    from oracle.oracle import Reference
-    steps = args.steps + args.warmup
-    t_total = 0.0
-    vals = []
-    # one measurement per step (warmup steps untimed)
+    step, cores, kind = cpu_stepper(params)
     r, vr, ell, ids = state
+    n = len(r)
     cur = (r, vr, ell, ids.astype(np.float64))
-    kind = res["kind"]
-    if kind == "reference":
-        R = Reference(fast=True)
-
-        def step(c):
-            if params.get("method") == 2:
-                tab, _ = R.step_kdk(c[0], c[1], c[2], c[3], params["dt"], parallel_sort=True)
-            else:
-                tab, _ = R.step_method5(c[0], c[1], c[2], c[3], params["dt"], max_subdiv=params["max_subdiv"],
-                                        lc_rule=params["lc_rule"], lc_radius=params["lc_radius"],
-                                        parallel_sort=True)
-            return tab[0], tab[1], tab[2], tab[3]
-    else:
-        from oracle.oracle import Oracle
-        O = Oracle()
-        op = O.params(dt=params["dt"], max_subdiv=params.get("max_subdiv", 128),
-                      lc_rule=params.get("lc_rule", 0), lc_radius=params.get("lc_radius", 1e-3))
-
-        def step(c):
-            return O.step_kdk(op, *c) if params.get("method") == 2 else O.step_adaptive(op, *c)[:4]
-    # bound the run: at most ~3 minutes of CPU time in total
-    budget = 180.0
-    done = 0
-    for j in range(steps):
+    budget, t_total, done = 180.0, 0.0, 0
+    for j in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         cur = step(cur)
         dt_ = time.perf_counter() - t0
         if j >= args.warmup:
             t_total += dt_
             done += 1
-        if t_total > budget and done >= 1:
-            break
-        vals.append(dt_)
-    n = len(r)
+            if t_total > budget:
+                break
     value = n * done / t_total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / done, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ICs)",
-        "config": cfg,
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["cores"], "kind": kind,
-                         "sample": "%d timed steps of the full N=%d state after %d warm-up steps" % (done, n, args.warmup)},
+        "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / done,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded ICs)", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": "%d timed full steps of the N=%d state after %d warm-up steps"
+                                   % (done, n, args.warmup)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -243,13 +223,12 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    cfg, state, params = workload(args)
-    if world > 1:
-        # independent replica per rank (the path does not shard across GPUs)
-        from nsphere_gb300 import ics
-        state = ics.hernquist(args.n, seed=2 + rank) if args.workload == "adaptive" else ics.plummer(args.n, seed=1 + rank)
+    # independent replica per rank (the path does not shard across GPUs)
+    cfg, state, params = workload(args, seed_offset=rank)
     r, vr, ell, ids = state
     n = len(r)
+    fp64 = ns.probe_fp64()
+
     # a dedicated (non-default) stream shared by the library and the timing events
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -287,23 +266,33 @@ def main():
     status = ctx.status()
 
     # per-kernel breakdown from the library's own CUDA events (short profiled pass)
+    nprof = 3
     ctx.profile(True)
-    ctx.step(3)
+    ctx.step(nprof)
     prof = ctx.profile_read()
     ctx.profile(False)
+
+    # the sort + scan + force pass on its own: fixed-step leapfrog steps of the same
+    # state (kick + drift, then bucket sort and the gather that writes the rank force)
+    kp = ns.default_params(dt=params["dt"], method=ns.METHOD_KDK)
+    ctx.set_params(kp)
+    ctx.step(2)
+    ctx.profile(True)
+    ctx.step(nprof)
+    kprof = ctx.profile_read()
+    ctx.profile(False)
+    ctx.set_params(p)
 
     # end to end through the public C ABI with host buffers: upload (pinned), step, download
     pin = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(8)]
     h_r, h_v, h_l, h_i, o_r, o_v, o_l, o_i = [t.numpy() for t in pin]
     h_r[:], h_v[:], h_l[:], h_i[:] = r, vr, ell, ids
     lib = ns.lib()
-    import ctypes as C
 
     def P(a):
         return C.c_void_p(a.ctypes.data)
 
     barrier()
-    t0 = time.perf_counter()
     ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ee0.record(stream)
     for _ in range(args.e2e_steps):
@@ -312,31 +301,41 @@ def main():
         ctx._check(lib.nsg_download(ctx.handle, P(o_r), P(o_v), P(o_l), P(o_i), None))
     ee1.record(stream)
     barrier()
-    e2e_ms = ee0.elapsed_time(ee1)
-    et = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+    et = torch.tensor([ee0.elapsed_time(ee1)], dtype=torch.float64, device="cuda")
     if world > 1:
         dist.all_reduce(et, op=dist.ReduceOp.MAX)
     e2e_value = n * world * args.e2e_steps / (float(et.item()) / 1e3)
 
     if rank == 0:
-        tot = sum(k["total_ms"] for k in prof) or 1.0
-        dom = max(prof, key=lambda k: k["total_ms"]) if prof else None
         peaks = {}
         try:
             peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         except Exception:
             pass
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
-        peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-        sort_ms = sum(k["total_ms"] for k in prof if k["name"] in ("sort_seed", "sort_radix", "rank_force")) / 3
-        sort_gbs = HBM_BYTES_SORT * n / (sort_ms / 1e3) / 1e9 if sort_ms else None
+        peak_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in peaks else "fallback"
+        by = {k["name"]: k for k in prof}
+        kby = {k["name"]: k for k in kprof}
+        main_ms = sum(k["total_ms"] for k in prof if k["name"] != "levi_civita") / nprof
+        tot = sum(k["total_ms"] for k in prof) or 1.0
         roof = None
-        if dom is not None:
-            per_launch = dom["total_ms"] / dom["launches"]
-            ach = (dom["bytes"] / dom["launches"]) / (per_launch / 1e3) / 1e9
-            roof = {"bound": "hbm", "kernel": dom["name"], "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": ach / hbm_peak, "traffic": None, "peak_source": peak_src,
-                    "share": dom["total_ms"] / tot}
+        if "gather_level0" in by:
+            g = by["gather_level0"]
+            per = g["total_ms"] / g["launches"]
+            ach = (g["bytes"] / g["launches"]) / (per / 1e3) / 1e9
+            flops = LEVEL0_FLOPS * n / (per / 1e3) / 1e12
+            roof = {"bound": "hbm", "kernel": "k_gather_level0", "achieved": ach, "peak": hbm_peak,
+                    "unit": "GB/s", "frac": ach / hbm_peak, "traffic": GATHER_LEVEL0_TRAFFIC * n,
+                    "peak_source": peak_src,
+                    "note": "compute-bound on the FP64 pipe (ncu: 75% FP64 pipe active); "
+                            "FP64 view below",
+                    "fp64": {"achieved_tflops": flops, "peak_tflops": fp64["dfma_tflops"],
+                             "frac": flops / fp64["dfma_tflops"],
+                             "peak_source": "measured live by nsg_probe_fp64 (FMA = 2 flops)"}}
+        sort_names = ["bucket_scatter", "bucket_sort", "sort_seed", "sort_radix", "gather_kick"]
+        sort_ms = sum(kby[k]["total_ms"] for k in sort_names if k in kby) / nprof
+        sort_gbs = SORT_PASS_BYTES * n / (sort_ms / 1e3) / 1e9 if sort_ms else None
+        lc = by.get("levi_civita")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -346,16 +345,27 @@ def main():
                     "d2h_bytes_per_step": 32 * n},
             "gpu_launches": int(l1 - l0),
             "roofline": roof,
-            "sort_scan_force": {"ms": sort_ms, "GBps": sort_gbs, "frac": (sort_gbs / hbm_peak) if sort_gbs else None,
-                                "bytes_per_particle": HBM_BYTES_SORT},
-            "kernels": [{"name": k["name"], "ms_per_step": k["total_ms"] / 3, "share": k["total_ms"] / tot}
+            "critical_path": {
+                "levi_civita_ms": (lc["total_ms"] / lc["launches"]) if lc else 0.0,
+                "main_stream_ms": main_ms,
+                "note": "Levi-Civita particles run as serial chains on a side stream; the step ends "
+                        "when the longest chain ends",
+                "fp64_dependent_latency_cycles": {"fma": fp64["fma_latency_cycles"],
+                                                  "division": fp64["div_latency_cycles"]}},
+            "sort_scan_force": {"ms": sort_ms, "GBps": sort_gbs,
+                                "frac": (sort_gbs / hbm_peak) if sort_gbs else None,
+                                "bytes_per_particle": SORT_PASS_BYTES,
+                                "kernels": [k for k in sort_names if k in kby]},
+            "kernels": [{"name": k["name"], "ms_per_step": k["total_ms"] / nprof, "share": k["total_ms"] / tot}
                         for k in prof],
+            "fp64_probe": fp64,
             "energy_drift": abs(E1 - E0) / abs(E0),
+            "energy_drift_steps": args.warmup + args.steps,
             "level_hist": [int(x) for x in hist],
             "status": status,
         }
         if not args.no_cpu_baseline and world == 1:
-            line["cpu_baseline"] = cpu_baseline(state, params, args, args.cpu_seconds)
+            line["cpu_baseline"] = cpu_baseline(state, params, args.cpu_seconds)
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:

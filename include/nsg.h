@@ -169,6 +169,14 @@ int nsg_clear_status(nsg_ctx *ctx);
 int nsg_selftest_division(uint64_t seed, int64_t count, int64_t *mismatches,
                           int64_t *fast_path, double *first_bad);
 
+/* Diagnostic without a reference counterpart: FP64 figures of the current device
+ * used as roofline denominators for the FP64-bound integrators (any pointer may be
+ * NULL): FMA throughput in TFLOP/s, IEEE division throughput on the FP64 pipe and on
+ * the integer pipe in G divisions/s, and single-warp dependent latency of one FMA
+ * and one division in cycles. */
+int nsg_probe_fp64(double *dfma_tflops, double *div_hw_gps, double *div_int_gps,
+                   double *fma_latency_cycles, double *div_latency_cycles);
+
 /* Kernels launched by steps and sorts so far, and steps taken (for reporting). */
 int nsg_counters(nsg_ctx *ctx, int64_t *launches, int64_t *steps);
 

@@ -30,7 +30,7 @@ EXPORTS = [
     "nsg_sort", "nsg_download", "nsg_download_particles", "nsg_device_state",
     "nsg_sort_particles", "nsg_gather", "nsg_energy", "nsg_level_hist", "nsg_levels",
     "nsg_sync", "nsg_status", "nsg_clear_status", "nsg_profile", "nsg_profile_read", "nsg_counters",
-    "nsg_selftest_division",
+    "nsg_selftest_division", "nsg_probe_fp64",
 ]
 
 
@@ -89,6 +89,7 @@ def lib() -> C.CDLL:
         "nsg_profile": [P, C.c_int],
         "nsg_counters": [P, C.POINTER(I64), C.POINTER(I64)],
         "nsg_selftest_division": [C.c_uint64, I64, C.POINTER(I64), C.POINTER(I64), P],
+        "nsg_probe_fp64": [C.POINTER(D)] * 5,
         "nsg_profile_read": [P, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)],
     }
     for name, args in sig.items():
@@ -248,6 +249,16 @@ def selftest_division(count: int, seed: int = 1):
     if rc != NSG_OK:
         raise NsgError(rc, lib().nsg_last_error(None).decode())
     return mism.value, fast.value, tuple(first)
+
+
+def probe_fp64() -> dict:
+    """FP64 throughput and latency of the current GPU (see nsg_probe_fp64)."""
+    vals = [C.c_double() for _ in range(5)]
+    rc = lib().nsg_probe_fp64(*[C.byref(v) for v in vals])
+    if rc != NSG_OK:
+        raise NsgError(rc, lib().nsg_last_error(None).decode())
+    keys = ["dfma_tflops", "div_hw_gps", "div_int_gps", "fma_latency_cycles", "div_latency_cycles"]
+    return {k: v.value for k, v in zip(keys, vals)}
 
 
 def sort_particles(ctx: Context, particles: np.ndarray):

@@ -33,18 +33,19 @@ int grid_for(nsg_ctx *c, int64_t n, int threads, int per_sm)
     return (int)(want < cap ? want : cap);
 }
 
-ProfScope::ProfScope(nsg_ctx *c_, const char *name_, double bytes_) : c(c_), name(name_), bytes(bytes_)
+ProfScope::ProfScope(nsg_ctx *c_, const char *name_, double bytes_, cudaStream_t stream)
+    : c(c_), name(name_), bytes(bytes_), st(stream ? stream : c_->stream)
 {
     if (!c->profiling) return;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    cudaEventRecord(e0, c->stream);
+    cudaEventRecord(e0, st);
 }
 
 ProfScope::~ProfScope()
 {
     if (!c->profiling || !e0) return;
-    cudaEventRecord(e1, c->stream);
+    cudaEventRecord(e1, st);
     c->ev_pool.push_back(e0);
     c->ev_pool.push_back(e1);
     // the name and bytes ride along: stats are resolved at flush time
@@ -61,6 +62,7 @@ void prof_flush(nsg_ctx *c)
     std::vector<KernelStat> merged;
     size_t ev = 0;
     cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(c->side);
     for (auto &ks : c->stats) {
         if (ks.launches != -1) { merged.push_back(ks); continue; }
         float ms = 0.f;

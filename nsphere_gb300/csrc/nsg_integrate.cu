@@ -464,6 +464,7 @@ int integrate_adaptive(nsg_ctx *c)
         e = cudaEventRecord(c->ev_fork, s);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
         if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
+        ProfScope ps(c, "levi_civita", 0.0, c->side);
         k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, c->side>>>(a);
         // one warp per block, so consecutive particles land on different SMs: a
         // warp-wide FP64 instruction occupies an SM's FP64 pipe for many cycles,

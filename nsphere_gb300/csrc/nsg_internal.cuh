@@ -190,8 +190,9 @@ struct ProfScope {
     nsg_ctx *c;
     const char *name;
     double bytes;
+    cudaStream_t st;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    ProfScope(nsg_ctx *c_, const char *name_, double bytes_);
+    ProfScope(nsg_ctx *c_, const char *name_, double bytes_, cudaStream_t stream = nullptr);
     ~ProfScope();
 };
 void prof_flush(nsg_ctx *c);

@@ -177,6 +177,32 @@ int nsg_selftest_division(uint64_t seed, int64_t count, int64_t *mismatches,
 int nsg_probe_fp64(double *dfma_tflops, double *div_hw_gps, double *div_int_gps,
                    double *fma_latency_cycles, double *div_latency_cycles);
 
+/* ---- learned level scheduler (no reference counterpart: an addition of this
+ * library).  A 4 -> 64 -> 64 -> 8 MLP with BF16 weights and FP32 accumulation
+ * predicts from (r, v_r, ell, local dynamical time) the adaptive-leapfrog level each
+ * particle will accept.  With params.sched = NSG_SCHED_LEARNED a particle predicted
+ * to need level >= 1 skips the level-0 pass; every level is still tested from 0
+ * upward, so results are bit-identical to NSG_SCHED_PLAIN. */
+int nsg_mlp_num_params(void);
+/* Random initial weights (seeded); allocates the network on the context. */
+int nsg_mlp_init(nsg_ctx *ctx, uint64_t seed);
+int nsg_mlp_set_weights(nsg_ctx *ctx, const float *w, int64_t count);
+int nsg_mlp_get_weights(nsg_ctx *ctx, float *w, int64_t count);
+/* Runs nsteps plain adaptive steps and appends (features, accepted level) of every
+ * particle that needed level >= 1 and of level-0 particles with probability
+ * keep_level0 to a device-resident training set of `capacity` samples. */
+int nsg_mlp_collect(nsg_ctx *ctx, int nsteps, double keep_level0, int64_t capacity);
+/* Size of the training set (and up to max samples copied to X[.][4], y[.]). */
+int nsg_mlp_dataset(nsg_ctx *ctx, int64_t *count, float *X, int8_t *y, int64_t max);
+/* Adam on the GPU over the training set (level-0 samples weighted 1/keep_level0). */
+int nsg_mlp_train(nsg_ctx *ctx, int epochs, int batch, float lr, uint64_t seed, double *final_loss);
+/* Forward + backward of the class-weighted softmax cross-entropy summed over nb
+ * samples; grad receives nsg_mlp_num_params() floats (summed over samples). */
+int nsg_mlp_grad(nsg_ctx *ctx, const float *X, const int8_t *y, int64_t nb, const float *cls_w,
+                 float *grad, double *loss);
+/* Predicted class (and the 8 logits, may be NULL) of nb feature vectors. */
+int nsg_mlp_predict(nsg_ctx *ctx, const float *X, int64_t nb, int8_t *cls, float *logits);
+
 /* Kernels launched by steps and sorts so far, and steps taken (for reporting). */
 int nsg_counters(nsg_ctx *ctx, int64_t *launches, int64_t *steps);
 

@@ -31,6 +31,8 @@ EXPORTS = [
     "nsg_sort_particles", "nsg_gather", "nsg_energy", "nsg_level_hist", "nsg_levels",
     "nsg_sync", "nsg_status", "nsg_clear_status", "nsg_profile", "nsg_profile_read", "nsg_counters",
     "nsg_selftest_division", "nsg_probe_fp64",
+    "nsg_mlp_num_params", "nsg_mlp_init", "nsg_mlp_set_weights", "nsg_mlp_get_weights",
+    "nsg_mlp_collect", "nsg_mlp_dataset", "nsg_mlp_train", "nsg_mlp_grad", "nsg_mlp_predict",
 ]
 
 
@@ -90,6 +92,14 @@ def lib() -> C.CDLL:
         "nsg_counters": [P, C.POINTER(I64), C.POINTER(I64)],
         "nsg_selftest_division": [C.c_uint64, I64, C.POINTER(I64), C.POINTER(I64), P],
         "nsg_probe_fp64": [C.POINTER(D)] * 5,
+        "nsg_mlp_init": [P, C.c_uint64],
+        "nsg_mlp_set_weights": [P, P, I64],
+        "nsg_mlp_get_weights": [P, P, I64],
+        "nsg_mlp_collect": [P, C.c_int, D, I64],
+        "nsg_mlp_dataset": [P, C.POINTER(I64), P, P, I64],
+        "nsg_mlp_train": [P, C.c_int, C.c_int, C.c_float, C.c_uint64, C.POINTER(D)],
+        "nsg_mlp_grad": [P, P, P, I64, P, P, C.POINTER(D)],
+        "nsg_mlp_predict": [P, P, I64, P, P],
         "nsg_profile_read": [P, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)],
     }
     for name, args in sig.items():
@@ -100,6 +110,8 @@ def lib() -> C.CDLL:
     L.nsg_destroy.restype = None
     L.nsg_last_error.argtypes = [P]
     L.nsg_last_error.restype = C.c_char_p
+    L.nsg_mlp_num_params.argtypes = []
+    L.nsg_mlp_num_params.restype = C.c_int
     _lib = L
     return L
 
@@ -223,6 +235,52 @@ class Context:
 
     def clear_status(self):
         self._check(self._L.nsg_clear_status(self._h))
+
+    # ---- learned level scheduler
+    def mlp_init(self, seed: int = 1):
+        self._check(self._L.nsg_mlp_init(self._h, seed))
+
+    def mlp_weights(self):
+        w = np.zeros(self._L.nsg_mlp_num_params(), dtype=np.float32)
+        self._check(self._L.nsg_mlp_get_weights(self._h, _ptr(w), w.size))
+        return w
+
+    def mlp_set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._check(self._L.nsg_mlp_set_weights(self._h, _ptr(w), w.size))
+
+    def mlp_collect(self, nsteps: int, keep_level0: float = 0.01, capacity: int = 1 << 20):
+        self._check(self._L.nsg_mlp_collect(self._h, int(nsteps), float(keep_level0), int(capacity)))
+
+    def mlp_dataset(self, max_samples: int | None = None):
+        cnt = C.c_int64()
+        self._check(self._L.nsg_mlp_dataset(self._h, C.byref(cnt), None, None, 0))
+        k = cnt.value if max_samples is None else min(cnt.value, max_samples)
+        X = np.zeros((k, 4), dtype=np.float32)
+        y = np.zeros(k, dtype=np.int8)
+        self._check(self._L.nsg_mlp_dataset(self._h, C.byref(cnt), _ptr(X), _ptr(y), k))
+        return X, y
+
+    def mlp_train(self, epochs: int, batch: int = 1024, lr: float = 3e-3, seed: int = 1) -> float:
+        loss = C.c_double()
+        self._check(self._L.nsg_mlp_train(self._h, int(epochs), int(batch), C.c_float(lr), seed, C.byref(loss)))
+        return loss.value
+
+    def mlp_grad(self, X, y, cls_w):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.int8)
+        cw = np.ascontiguousarray(cls_w, dtype=np.float32)
+        g = np.zeros(self._L.nsg_mlp_num_params(), dtype=np.float32)
+        loss = C.c_double()
+        self._check(self._L.nsg_mlp_grad(self._h, _ptr(X), _ptr(y), X.shape[0], _ptr(cw), _ptr(g), C.byref(loss)))
+        return loss.value, g
+
+    def mlp_predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        cls = np.zeros(X.shape[0], dtype=np.int8)
+        lg = np.zeros((X.shape[0], 8), dtype=np.float32)
+        self._check(self._L.nsg_mlp_predict(self._h, _ptr(X), X.shape[0], _ptr(cls), _ptr(lg)))
+        return cls, lg
 
     def counters(self):
         a, b = C.c_int64(), C.c_int64()

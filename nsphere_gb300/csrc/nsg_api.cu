@@ -357,6 +357,7 @@ void nsg_destroy(nsg_ctx *c)
     if (c->side) cudaStreamSynchronize(c->side);
     for (auto ev : c->ev_pool) cudaEventDestroy(ev);
     free_buffers(c);
+    mlp_free(c);
     if (c->ctr) cudaFree(c->ctr);
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);

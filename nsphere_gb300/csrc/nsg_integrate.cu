@@ -30,6 +30,8 @@
 
 namespace nsg {
 
+constexpr uint32_t kFreshBit = 0x80000000u;   // queue entry that skipped level 0
+
 struct StepArgs {
     // sorted copy: k_gather_level0 writes it; final (r, v) land in r_out / v_out
     double *r_out, *v_out, *ell_out, *aux_out;
@@ -51,9 +53,10 @@ struct StepArgs {
     int N_taumin;
     int64_t max_tau_steps;
     DevCounters *ctr;
-    uint32_t *q_idx;            // particles that failed level 0
+    uint32_t *q_idx;            // particles that left level 0 (kFreshBit: skipped it)
     double *q_r, *q_v;          // their fine N=1 result (the coarse pass of level 1)
     uint32_t *lc_idx;
+    const int8_t *pred;         // learned schedule: predicted level per position, or null
     // Substep sizes of each pass, identical for every particle, computed once on
     // the host with the same IEEE divisions as nsphere.c:1566-1577 (exact here:
     // h divided by powers of two): coarse N=1 halfKick h/2, midStep h;
@@ -144,62 +147,80 @@ __global__ void __launch_bounds__(256) k_gather_level0(StepArgs a)
         const double gn = gnum_of(i, a.n, a.G, a.M, Mpt);
         const double l2 = dmul(ell, ell);
         const double af = acc_leap(r, gn, l2);
-        double rc, vc, rf, vf;
-        micro_leap<false>(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
-        micro_leap<false>(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
-        const bool ok = converged<false>(rc, vc, rf, vf, rf, a.tol_r, a.tol_v);
-        const bool bad = !(isfinite(rf) && isfinite(vf));
-        const bool done = ok || last || bad;
-        if (done) {
-            double ro, vo;
-            select_out(a.out_type, rc, vc, rf, vf, ro, vo);
-            a.r_out[i] = ro;
-            a.v_out[i] = vo;
-            a.level[i] = ok ? 0 : kLevelNotConverged;
-            if (!ok) atomicOr(&a.ctr->status, bad ? (NSG_ST_NAN | NSG_ST_NOT_CONVERGED) : NSG_ST_NOT_CONVERGED);
+        // learned schedule: a particle predicted to need level >= 1 goes straight to
+        // the level-parallel kernel, which tests every level from 0 upward
+        const bool fresh = (a.pred != nullptr) && !last && a.pred[i] >= 1;
+        double rc = 0.0, vc = 0.0, rf = 0.0, vf = 0.0;
+        bool done = false;
+        if (!fresh) {
+            micro_leap<false>(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
+            micro_leap<false>(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
+            const bool ok = converged<false>(rc, vc, rf, vf, rf, a.tol_r, a.tol_v);
+            const bool bad = !(isfinite(rf) && isfinite(vf));
+            done = ok || last || bad;
+            if (done) {
+                double ro, vo;
+                select_out(a.out_type, rc, vc, rf, vf, ro, vo);
+                a.r_out[i] = ro;
+                a.v_out[i] = vo;
+                a.level[i] = ok ? 0 : kLevelNotConverged;
+                if (!ok) atomicOr(&a.ctr->status, bad ? (NSG_ST_NAN | NSG_ST_NOT_CONVERGED) : NSG_ST_NOT_CONVERGED);
+            }
         }
         const int q = warp_append(!done, &a.ctr->qcount[1]);
         if (!done) {
             a.r_out[i] = r;          // start values for the higher levels
             a.v_out[i] = v;
             a.a0[i] = af;
-            a.q_idx[q] = (uint32_t)i;
+            a.q_idx[q] = fresh ? ((uint32_t)i | kFreshBit) : (uint32_t)i;
             a.q_r[q] = rf;
             a.q_v[q] = vf;
         }
     }
 }
 
-// Levels 1 .. nlev-1 for the particles queued by level 0.  A group of G lanes
-// (G = a power of two >= nlev-1) serves one particle; lane j runs the fine pass of
-// level k = j+1 (2^(k+1) drift-kick pairs).  All lanes advance one pair per
-// iteration, so level k's pass ends at iteration 2^(k+1): its test then uses the
-// pass of level k-1 (lane j-1, or the queued level-0 result for k = 1), in the
-// reference's order, and the group stops at the first level that passes.
+// Particles that leave level 0.  A group of G lanes (a power of two) serves one
+// particle and every lane runs one pass of it at the same time:
+//   plain layout (FULL = false; the particle failed level 0, whose fine pass is
+//     queued): lane j runs the fine pass of level j+1, G >= nlev-1;
+//   full layout (learned schedule; some particles skipped level 0): lane 0 runs
+//     the coarse N=1 pass, lane j >= 1 the fine pass of level j-1, G >= nlev+1.
+// All lanes advance one drift-kick pair per iteration, so the fine pass of level L
+// ends at iteration 2^(L+1); the test of level L then compares it with the pass
+// below it, levels in the reference's order, and the group stops at the first
+// level that passes (or the last level).
+template <bool FULL>
 __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
 {
     const unsigned cnt = a.ctr->qcount[1];
     if (cnt == 0) return;
     const double Mpt = a.ctr->point_mass;
     const int lane = threadIdx.x & 31;
-    const int j = lane & (G - 1);              // this lane runs level j+1
+    const int j = lane & (G - 1);              // pass of this lane within its group
     const int g0 = lane & ~(G - 1);            // first lane of the group
     const int groups_per_warp = 32 / G;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int nl = a.nlev - 1;                 // levels run here
-    const bool mine = j < nl;
-    const int k = j + 1;
-    const int64_t pairs = mine ? ((int64_t)2 << k) : 0;
-    const double hk = mine ? a.hk_f[k] : 0.0, ms = mine ? a.ms_f[k] : 0.0;
+    const int nl = a.nlev - 1;                 // highest level
+    int64_t pairs = 0;
+    double hk = 0.0, ms = 0.0;
+    if (FULL) {
+        if (j == 0) { pairs = 1; hk = a.hk_c0; ms = a.ms_c0; }
+        else if (j <= a.nlev) { pairs = (int64_t)1 << j; hk = a.hk_f[j - 1]; ms = a.ms_f[j - 1]; }
+    } else if (j < nl) {
+        pairs = (int64_t)2 << (j + 1); hk = a.hk_f[j + 1]; ms = a.ms_f[j + 1];
+    }
     for (int64_t round = 0;; round++) {
         const int64_t e = (round * warps + gw) * groups_per_warp + (lane / G);
         if (__all_sync(0xffffffffu, e >= (int64_t)cnt)) break;
         const bool have = e < (int64_t)cnt;
         uint32_t i = 0;
+        int kstart = 1;                        // first level this group tests
         double v_in = 0.0, l2 = 0.0, gn = 0.0, af = 0.0, rq = 0.0, vq = 0.0, r = 0.0;
         if (have) {
-            i = a.q_idx[e];
+            const uint32_t raw = a.q_idx[e];
+            i = raw & ~kFreshBit;
+            if (raw & kFreshBit) kstart = 0;
             r = a.r_out[i];
             v_in = a.v_out[i];
             const double ell = a.ell_out[i];
@@ -213,7 +234,7 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
         double v = dadd(v_in, dmul(hk, af));
         double rf = 0.0, vf = 0.0;             // this lane's finished pass
         int64_t it = 0;
-        int kcheck = 1;                        // next level to test
+        int kcheck = FULL ? 0 : 1;             // level tested next (same in every group)
         while (__any_sync(0xffffffffu, active)) {
             // one drift-kick pair; the last pair of a pass ends with the half-kick
             if (active && it < pairs) {
@@ -222,17 +243,17 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
                 else { v = dadd(v, dmul(hk, acc_leap<true>(r, gn, l2))); rf = r; vf = v; }
             }
             it++;
-            // level kcheck's pass (lane kcheck-1 of the group) ended at it = 2^(kcheck+1)
+            // the fine pass of level kcheck ended at it = 2^(kcheck+1)
             if (kcheck <= nl && it == ((int64_t)2 << kcheck)) {
-                const int srcF = g0 + kcheck - 1;
-                const int srcC = kcheck > 1 ? srcF - 1 : srcF;
+                const int srcF = FULL ? g0 + kcheck + 1 : g0 + kcheck - 1;
+                const int srcC = FULL ? g0 + kcheck : (kcheck > 1 ? srcF - 1 : srcF);
                 const double rF = __shfl_sync(0xffffffffu, rf, srcF);
                 const double vF = __shfl_sync(0xffffffffu, vf, srcF);
                 const double rC0 = __shfl_sync(0xffffffffu, rf, srcC);
                 const double vC0 = __shfl_sync(0xffffffffu, vf, srcC);
-                const double rC = (kcheck == 1) ? rq : rC0;
-                const double vC = (kcheck == 1) ? vq : vC0;
-                if (active) {
+                const double rC = (!FULL && kcheck == 1) ? rq : rC0;
+                const double vC = (!FULL && kcheck == 1) ? vq : vC0;
+                if (active && kcheck >= kstart) {
                     const bool ok = converged<true>(rC, vC, rF, vF, rF, a.tol_r, a.tol_v);
                     const bool bad = !(isfinite(rF) && isfinite(vF));
                     if (ok || bad || kcheck == nl) {
@@ -446,6 +467,7 @@ static StepArgs make_args(nsg_ctx *c)
     a.ctr = c->ctr;
     a.q_idx = c->q_idx[0]; a.q_r = c->q_r[0]; a.q_v = c->q_v[0];
     a.lc_idx = c->lc_idx;
+    a.pred = nullptr;
     return a;
 }
 
@@ -453,6 +475,11 @@ int integrate_adaptive(nsg_ctx *c)
 {
     if (int rc = sort_perm(c)) return rc;
     StepArgs a = make_args(c);
+    const bool learned = (c->p.sched == NSG_SCHED_LEARNED) && a.nlev > 1;
+    if (learned)
+        if (int rc = mlp_predict_sorted(c, &a.pred)) return rc;
+    if (c->mlp_collect)
+        if (int rc = mlp_features_sorted(c)) return rc;
     cudaStream_t s = c->stream;
     cudaError_t e;
     // reset queue counters (qcount[] and lc_count live at the head of DevCounters)
@@ -485,14 +512,17 @@ int integrate_adaptive(nsg_ctx *c)
     if (a.nlev > 1) {
         ProfScope ps(c, "leap_levels", 0.0);
         int G = 1;
-        while (G < a.nlev - 1) G <<= 1;
-        k_levels_lanes<<<c->num_sms * 4, 256, 0, s>>>(a, G);
+        while (G < (learned ? a.nlev + 1 : a.nlev - 1)) G <<= 1;
+        if (learned) k_levels_lanes<true><<<c->num_sms * 4, 256, 0, s>>>(a, G);
+        else k_levels_lanes<false><<<c->num_sms * 4, 256, 0, s>>>(a, G);
         c->launches += 1;
     }
     if (lc) {
         e = cudaStreamWaitEvent(s, c->ev_join, 0);
         if (e != cudaSuccess) return cuda_err(c, e, "join wait");
     }
+    if (c->mlp_collect)
+        if (int rc = mlp_append_levels(c)) return rc;
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(c, e, "integrator kernels");
     c->cur = 1 - c->cur;

@@ -36,6 +36,8 @@ struct DevCounters {
     unsigned int pad;
 };
 
+struct MlpDev;   // nsg_mlp.cu
+
 struct KernelStat {
     std::string name;
     int64_t launches = 0;
@@ -95,6 +97,10 @@ struct nsg_ctx {
 
     // staging for uploads of ids given as doubles
     double *stage_d = nullptr;
+
+    // learned level scheduler (nsg_mlp.cu)
+    nsg::MlpDev *mlp = nullptr;
+    bool mlp_collect = false;        // record (features, level) of each step
 
     bool profiling = false;
     std::vector<nsg::KernelStat> stats;
@@ -205,6 +211,10 @@ int integrate_adaptive(nsg_ctx *c);                   // method 3 / 5: sort_perm
 int kdk_first_half(nsg_ctx *c);                       // kick (a0 of the current rank) + drift
 int compute_energy(nsg_ctx *c);                       // K, W of the sorted live copy
 int bucket_sort_perm(nsg_ctx *c);                     // near-sorted fast path (sets need_fallback)
+int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred);  // predicted level per sorted position
+int mlp_features_sorted(nsg_ctx *c);                  // features of the sort (training set)
+int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)
+void mlp_free(nsg_ctx *c);
 int bucket_setup(nsg_ctx *c);
 int launch_gather(nsg_ctx *c, const int32_t *d_ids, int k, double *d_out, int32_t *d_rank);
 int launch_level_hist(nsg_ctx *c);

@@ -794,6 +794,8 @@ int nsg_mlp_grad(nsg_ctx *c, const float *X, const int8_t *y, int64_t nb, const 
 {
     if (!c || !X || !y || nb <= 0 || !cls_w) return set_err(c, NSG_EINVAL, "bad gradient arguments");
     if (!c->mlp || !c->mlp->ready) return set_err(c, NSG_ESTATE, "no network");
+    for (int64_t k = 0; k < nb; k++)
+        if (y[k] < 0 || y[k] >= kOut) return set_err(c, NSG_EINVAL, "class labels must be in 0..7");
     MlpDev *m = c->mlp;
     float *d_X = nullptr, *d_w = nullptr;
     int8_t *d_y = nullptr;

@@ -92,6 +92,10 @@ NSG_HD bool div_rn_fast(double a, double b, double *out)
 {
     const uint64_t ua = div_bits(a), ub = div_bits(b);
     const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+    if (eb - 1u < 2046u && (ua << 1) == 0ull) {              // +-0 / normal: signed zero
+        *out = div_from_bits((ua ^ ub) & (1ull << 63));
+        return true;
+    }
     if (ea - 1u >= 2046u || eb - 1u >= 2046u) return false;  // zero, subnormal, inf, NaN
     const uint64_t MANT = (1ull << 52) - 1ull, HID = 1ull << 52;
     const uint64_t ma = (ua & MANT) | HID, mb = (ub & MANT) | HID;
@@ -139,6 +143,17 @@ __device__ __forceinline__ double div_rn(double a, double b)
 {
     double q;
     if (div_rn_fast(a, b, &q)) return q;
+    return __ddiv_rn(a, b);
+}
+
+// The FP64 pipe's division with the +-0 / normal case answered directly (IEEE:
+// a zero with the sign a XOR b).  The innermost particle has a zero gravity
+// numerator, so its serial chains divide zero in every force evaluation.
+__device__ __forceinline__ double div_rn_hw(double a, double b)
+{
+    const uint64_t ua = div_bits(a), ub = div_bits(b);
+    const uint32_t eb = (uint32_t)(ub >> 52) & 0x7ffu;
+    if (eb - 1u < 2046u && (ua << 1) == 0ull) return div_from_bits((ua ^ ub) & (1ull << 63));
     return __ddiv_rn(a, b);
 }
 #endif

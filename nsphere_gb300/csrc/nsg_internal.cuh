@@ -121,7 +121,7 @@ __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a,
 // FP64 pipe's shorter dependent sequence.  Both are IEEE round-to-nearest, so
 // the choice never changes a result bit.
 template <bool HW>
-__device__ __forceinline__ double ddivx(double a, double b) { return HW ? __ddiv_rn(a, b) : div_rn(a, b); }
+__device__ __forceinline__ double ddivx(double a, double b) { return HW ? div_rn_hw(a, b) : div_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return div_rn(a, b); }
 
 // -(G) * (i / n) * M (+ the point-mass term when present), nsphere.c:513.

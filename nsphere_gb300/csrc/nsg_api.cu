@@ -207,6 +207,11 @@ __global__ void k_selftest_div(uint64_t seed, int64_t count, unsigned long long 
         double t = __ddiv_rn(a, b);
         fast += f;
         bool same = (__double_as_longlong(q) == __double_as_longlong(t)) || (q != q && t != t);
+        // signed zero dividends (the innermost particle's gravity numerator)
+        const double z = (h1 & 1) ? -0.0 : 0.0;
+        const double zq = div_rn(z, b), zh = div_rn_hw(z, b), zt = __ddiv_rn(z, b);
+        same = same && ((__double_as_longlong(zq) == __double_as_longlong(zt)) || (zq != zq && zt != zt));
+        same = same && ((__double_as_longlong(zh) == __double_as_longlong(zt)) || (zh != zh && zt != zt));
         if (!same && atomicAdd(&out[1], 1ull) == 0) { first[0] = a; first[1] = b; }
     }
     atomicAdd(&out[2], fast);

@@ -108,6 +108,17 @@ int nsg_get_params(nsg_ctx *ctx, nsg_params *p);
  * reference (its state is host-resident); the upload is the one H2D copy. */
 int nsg_upload(nsg_ctx *ctx, const double *r, const double *vr, const double *ell,
                const double *id_as_double, const double *aux, int64_t n);
+/* Ensemble of independent halos (no reference counterpart: the reference runs one
+ * halo per process).  Halo h is the next halo_n[h] rows of the columns; every halo
+ * is sorted, ranked (M_i = (i/N_h) M with its own N_h) and integrated on its own in
+ * the same launches.  ids: a permutation of 0..n-1 in which halo h owns the ids of
+ * its own row range. */
+int nsg_upload_ensemble(nsg_ctx *ctx, const double *r, const double *vr, const double *ell,
+                        const double *id_as_double, const double *aux, const int64_t *halo_n,
+                        int nhalo);
+int nsg_num_halos(nsg_ctx *ctx);
+/* Per-halo energies K[h], W[h] (arrays of nsg_num_halos entries). */
+int nsg_energy_halos(nsg_ctx *ctx, double *K, double *W);
 /* Same with the reference's double ** row table: particles[0..4]. */
 int nsg_upload_particles(nsg_ctx *ctx, double *const *particles, int64_t n);
 /* Same from device pointers (int32 ids). */

@@ -31,6 +31,7 @@ EXPORTS = [
     "nsg_sort_particles", "nsg_gather", "nsg_energy", "nsg_level_hist", "nsg_levels",
     "nsg_sync", "nsg_status", "nsg_clear_status", "nsg_profile", "nsg_profile_read", "nsg_counters",
     "nsg_selftest_division", "nsg_probe_fp64",
+    "nsg_upload_ensemble", "nsg_num_halos", "nsg_energy_halos",
     "nsg_mlp_num_params", "nsg_mlp_init", "nsg_mlp_set_weights", "nsg_mlp_get_weights",
     "nsg_mlp_collect", "nsg_mlp_dataset", "nsg_mlp_train", "nsg_mlp_grad", "nsg_mlp_predict",
 ]
@@ -92,6 +93,9 @@ def lib() -> C.CDLL:
         "nsg_counters": [P, C.POINTER(I64), C.POINTER(I64)],
         "nsg_selftest_division": [C.c_uint64, I64, C.POINTER(I64), C.POINTER(I64), P],
         "nsg_probe_fp64": [C.POINTER(D)] * 5,
+        "nsg_upload_ensemble": [P, P, P, P, P, P, P, C.c_int],
+        "nsg_num_halos": [P],
+        "nsg_energy_halos": [P, P, P],
         "nsg_mlp_init": [P, C.c_uint64],
         "nsg_mlp_set_weights": [P, P, I64],
         "nsg_mlp_get_weights": [P, P, I64],
@@ -187,6 +191,24 @@ class Context:
             raise ValueError("columns must have equal length")
         self._check(self._L.nsg_upload(self._h, _ptr(r), _ptr(vr), _ptr(ell), _ptr(idd), _ptr(aux), n))
         self.n = n
+
+    def upload_ensemble(self, r, vr, ell, ids, halo_n, aux=None):
+        """Independent halos in one state: halo h is the next halo_n[h] rows."""
+        r, vr, ell = (np.ascontiguousarray(x, dtype=np.float64) for x in (r, vr, ell))
+        idd = np.ascontiguousarray(ids, dtype=np.float64)
+        hn = np.ascontiguousarray(halo_n, dtype=np.int64)
+        aux = None if aux is None else np.ascontiguousarray(aux, dtype=np.float64)
+        if int(hn.sum()) != r.shape[0]:
+            raise ValueError("halo sizes must add up to the number of rows")
+        self._check(self._L.nsg_upload_ensemble(self._h, _ptr(r), _ptr(vr), _ptr(ell), _ptr(idd), _ptr(aux),
+                                                _ptr(hn), int(hn.size)))
+        self.n = r.shape[0]
+
+    def energy_halos(self):
+        nh = self._L.nsg_num_halos(self._h)
+        K, W = np.zeros(nh), np.zeros(nh)
+        self._check(self._L.nsg_energy_halos(self._h, _ptr(K), _ptr(W)))
+        return K, W
 
     def step(self, nsteps: int = 1):
         self._check(self._L.nsg_step(self._h, int(nsteps)))

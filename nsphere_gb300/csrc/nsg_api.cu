@@ -108,6 +108,17 @@ __global__ void k_count_ids(const int32_t *__restrict__ id, int64_t n, int32_t *
     }
 }
 
+// Ensembles: the particle at position p belongs to the halo whose position range
+// holds p, and its id must lie in that same range.
+__global__ void k_check_halo_ids(const int32_t *__restrict__ id, int64_t n, Seg sg, unsigned int *bad)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int h = seg_of(sg, k);
+        if (id[k] < sg.start[h] || id[k] >= sg.start[h + 1]) atomicOr(bad, 1u);
+    }
+}
+
 __global__ void k_check_counts(const int32_t *__restrict__ cnt, int64_t n, unsigned int *bad)
 {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
@@ -233,6 +244,8 @@ static void free_buffers(nsg_ctx *c)
     f(c->a0); f(c->inv); f(c->level); f(c->tile_counts); f(c->digit_tot); f(c->lc_idx);
     f(c->red_part); f(c->stage_d);
     f(c->split); f(c->bcnt); f(c->boff); f(c->bkey); f(c->bpay);
+    f(c->d_seg_start); f(c->d_bbase); f(c->seg_energy);
+    c->nb_cap = 0;
     c->cap = 0;
 }
 
@@ -255,9 +268,6 @@ static int ensure_capacity(nsg_ctx *c, int64_t n)
     A(c->a0, d8); A(c->inv, d4); A(c->level, (size_t)n);
     A(c->tile_counts, (size_t)ntiles * kRadixBuckets * 4); A(c->digit_tot, kRadixBuckets * 4);
     A(c->lc_idx, d4); A(c->red_part, 2 * kReduceBlocks * 8); A(c->stage_d, d8);
-    const size_t nb = (size_t)((n + kBucketTarget - 1) / kBucketTarget);
-    A(c->split, nb * 8); A(c->bcnt, nb * 4); A(c->boff, nb * 4);
-    A(c->bkey, nb * kBucketCap * 8); A(c->bpay, nb * kBucketCap * 8);
     if (e != cudaSuccess) {
         free_buffers(c);
         return cuda_err(c, e, "device allocation");
@@ -413,20 +423,66 @@ static int validate_ids(nsg_ctx *c, const int32_t *d_id, int64_t n, unsigned int
     if (e != cudaSuccess) return cuda_err(c, e, "id validation setup");
     k_count_ids<<<grid_for(c, n, 256), 256, 0, c->stream>>>(d_id, n, c->inv, d_bad);
     k_check_counts<<<grid_for(c, n, 256), 256, 0, c->stream>>>(c->inv, n, d_bad);
+    if (c->nseg > 1)
+        k_check_halo_ids<<<grid_for(c, n, 256), 256, 0, c->stream>>>(d_id, n, seg_table(c), d_bad);
     unsigned int bad = 0;
     e = cudaMemcpyAsync(&c->h_ctr->pad, d_bad, 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "id validation");
     bad = c->h_ctr->pad | bad_in;
-    if (bad) return set_err(c, NSG_EIDS, "particle ids must be a permutation of 0..n-1");
+    if (bad)
+        return set_err(c, NSG_EIDS, c->nseg > 1 ? "particle ids must be a permutation of 0..n-1 with each "
+                                                  "halo's ids in its own position range"
+                                                : "particle ids must be a permutation of 0..n-1");
     return NSG_OK;
 }
 
-static int upload_common(nsg_ctx *c, int64_t n)
+// Halo table of the resident state (one halo unless an ensemble was uploaded):
+// position ranges, near-sorted buckets per halo, per-halo energy slots.
+static int setup_segments(nsg_ctx *c, const int64_t *seg_n, int nseg)
+{
+    std::vector<int64_t> start((size_t)nseg + 1, 0);
+    std::vector<int32_t> bbase((size_t)nseg + 1, 0);
+    for (int h = 0; h < nseg; h++) {
+        if (seg_n[h] <= 0) return set_err(c, NSG_EINVAL, "every halo needs at least one particle");
+        start[h + 1] = start[h] + seg_n[h];
+        bbase[h + 1] = bbase[h] + (int32_t)((seg_n[h] + kBucketTarget - 1) / kBucketTarget);
+    }
+    if (start[nseg] != c->n) return set_err(c, NSG_EINVAL, "halo sizes must add up to n");
+    const int64_t nb = bbase[nseg];
+    auto F = [](auto *&p) { if (p) cudaFree((void *)p); p = nullptr; };
+    cudaError_t e = cudaSuccess;
+    if (nb > c->nb_cap) {
+        F(c->split); F(c->bcnt); F(c->boff); F(c->bkey); F(c->bpay);
+        e = cudaMalloc((void **)&c->split, (size_t)nb * 8);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&c->bcnt, (size_t)nb * 4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&c->boff, (size_t)nb * 4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&c->bkey, (size_t)nb * kBucketCap * 8);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&c->bpay, (size_t)nb * kBucketCap * 8);
+        if (e != cudaSuccess) return cuda_err(c, e, "bucket buffers");
+        c->nb_cap = nb;
+    }
+    F(c->d_seg_start); F(c->d_bbase); F(c->seg_energy);
+    e = cudaMalloc((void **)&c->d_seg_start, start.size() * 8);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_bbase, bbase.size() * 4);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->seg_energy, (size_t)2 * nseg * 8);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_seg_start, start.data(), start.size() * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_bbase, bbase.data(), bbase.size() * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_err(c, e, "halo table");
+    c->nseg = nseg;
+    c->h_seg_start = start;
+    c->nb_total = nb;
+    return NSG_OK;
+}
+
+static int upload_common(nsg_ctx *c, int64_t n, const int64_t *seg_n = nullptr, int nseg = 1)
 {
     if (n <= 0 || n > (int64_t)0x7fffffff) return set_err(c, NSG_EINVAL, "n must be in [1, 2^31-1]");
+    if (nseg < 1 || nseg > 65536) return set_err(c, NSG_EINVAL, "1 to 65536 halos");
     if (int rc = ensure_capacity(c, n)) return rc;
     c->n = n;
+    const int64_t one = n;
+    if (int rc = setup_segments(c, seg_n ? seg_n : &one, seg_n ? nseg : 1)) return rc;
     c->cur = 0;
     c->sorted = false;
     c->inv_valid = false;
@@ -434,13 +490,14 @@ static int upload_common(nsg_ctx *c, int64_t n)
     return NSG_OK;
 }
 
-int nsg_upload(nsg_ctx *c, const double *r, const double *vr, const double *ell,
-               const double *id_as_double, const double *aux, int64_t n)
+static int upload_host(nsg_ctx *c, const double *r, const double *vr, const double *ell,
+                       const double *id_as_double, const double *aux, int64_t n, const int64_t *seg_n,
+                       int nseg)
 {
     if (int rc = check_ctx(c)) return rc;
     if (!r || !vr || !ell || !id_as_double) return set_err(c, NSG_EINVAL, "null column");
     if (c->p.carry_aux && !aux) return set_err(c, NSG_EINVAL, "carry_aux set but aux is null");
-    if (int rc = upload_common(c, n)) return rc;
+    if (int rc = upload_common(c, n, seg_n, nseg)) return rc;
     const size_t b = (size_t)n * 8;
     cudaStream_t s = c->stream;
     cudaError_t e = cudaMemcpyAsync(c->r[0], r, b, cudaMemcpyHostToDevice, s);
@@ -452,6 +509,52 @@ int nsg_upload(nsg_ctx *c, const double *r, const double *vr, const double *ell,
     if (e != cudaSuccess) return cuda_err(c, e, "upload copy");
     k_ids_from_double<<<grid_for(c, n, 256), 256, 0, s>>>(c->stage_d, c->id[0], n, &c->ctr->pad);
     return validate_ids(c, c->id[0], n, 0);
+}
+
+int nsg_upload(nsg_ctx *c, const double *r, const double *vr, const double *ell,
+               const double *id_as_double, const double *aux, int64_t n)
+{
+    return upload_host(c, r, vr, ell, id_as_double, aux, n, nullptr, 1);
+}
+
+int nsg_upload_ensemble(nsg_ctx *c, const double *r, const double *vr, const double *ell,
+                        const double *id_as_double, const double *aux, const int64_t *halo_n, int nhalo)
+{
+    if (!halo_n || nhalo < 1) return set_err(c, NSG_EINVAL, "halo sizes missing");
+    int64_t n = 0;
+    for (int h = 0; h < nhalo; h++) n += halo_n[h];
+    return upload_host(c, r, vr, ell, id_as_double, aux, n, halo_n, nhalo);
+}
+
+int nsg_num_halos(nsg_ctx *c)
+{
+    return c ? c->nseg : 0;
+}
+
+int nsg_energy_halos(nsg_ctx *c, double *K, double *W)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
+    if (!c->sorted)
+        if (int rc = sort_state(c)) return rc;
+    if (int rc = compute_energy(c)) return rc;
+    if (c->nseg <= 1) {
+        cudaError_t e = cudaMemcpyAsync(c->h_ctr->energy, c->ctr->energy, 16, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_err(c, e, "energy readback");
+        if (K) K[0] = c->h_ctr->energy[0];
+        if (W) W[0] = c->h_ctr->energy[1];
+        return NSG_OK;
+    }
+    std::vector<double> h((size_t)2 * c->nseg);
+    cudaError_t e = cudaMemcpyAsync(h.data(), c->seg_energy, h.size() * 8, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "energy readback");
+    for (int k = 0; k < c->nseg; k++) {
+        if (K) K[k] = h[2 * k];
+        if (W) W[k] = h[2 * k + 1];
+    }
+    return NSG_OK;
 }
 
 int nsg_upload_particles(nsg_ctx *c, double *const *particles, int64_t n)

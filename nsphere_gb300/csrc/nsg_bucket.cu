@@ -27,15 +27,16 @@ constexpr int kBucketItems = 12;
 constexpr int kBucketWarps = kBucketThreads / 32;
 
 
-// Largest b with S[b] <= key (S[0] is the smallest key), searched from home.
-__device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int nb, uint64_t key, int home)
+// Largest b in [lo, hi) with S[b] <= key (S[lo] is the smallest key of the halo),
+// searched from home.
+__device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int lo0, int hi0, uint64_t key, int home)
 {
     int b = home;
     if (S[b] <= key) {
         int steps = 0;
-        while (b + 1 < nb && S[b + 1] <= key && steps < 8) { b++; steps++; }
-        if (b + 1 < nb && S[b + 1] <= key) {       // far move: binary search in (b, nb)
-            int lo = b + 1, hi = nb - 1;           // S[lo] <= key
+        while (b + 1 < hi0 && S[b + 1] <= key && steps < 8) { b++; steps++; }
+        if (b + 1 < hi0 && S[b + 1] <= key) {      // far move: binary search in (b, hi0)
+            int lo = b + 1, hi = hi0 - 1;          // S[lo] <= key
             while (lo < hi) {
                 int mid = (lo + hi + 1) >> 1;
                 if (S[mid] <= key) lo = mid; else hi = mid - 1;
@@ -44,9 +45,9 @@ __device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int n
         }
     } else {
         int steps = 0;
-        while (b > 0 && S[b] > key && steps < 8) { b--; steps++; }
-        if (S[b] > key) {                          // binary search in [0, b)
-            int lo = 0, hi = b - 1;                // S[0] <= key always
+        while (b > lo0 && S[b] > key && steps < 8) { b--; steps++; }
+        if (S[b] > key) {                          // binary search in [lo0, b)
+            int lo = lo0, hi = b - 1;              // S[lo0] <= key always
             while (lo < hi) {
                 int mid = (lo + hi + 1) >> 1;
                 if (S[mid] <= key) lo = mid; else hi = mid - 1;
@@ -59,7 +60,7 @@ __device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int n
 
 __global__ void __launch_bounds__(256)
 k_bucket_scatter(const double *__restrict__ r, const int32_t *__restrict__ id, int64_t n,
-                 const uint64_t *__restrict__ S, int nb, int B, int cap,
+                 const uint64_t *__restrict__ S, Seg sg, int B, int cap,
                  unsigned int *__restrict__ cnt, uint64_t *__restrict__ bkey,
                  uint64_t *__restrict__ bpay, DevCounters *ctr)
 {
@@ -69,9 +70,12 @@ k_bucket_scatter(const double *__restrict__ r, const int32_t *__restrict__ id, i
         double rp = r[p];
         nan_seen |= (rp != rp);
         uint64_t key = radius_key(rp);
-        int home = (int)(p / B);
-        if (home >= nb) home = nb - 1;
-        int b = find_bucket(S, nb, key, home);
+        // a particle stays in its halo: search that halo's buckets only
+        const Local L = local_of(sg, p, n);
+        const int lo = sg.bbase[L.h], hi = sg.bbase[L.h + 1];
+        int home = lo + (int)(L.i / B);
+        if (home >= hi) home = hi - 1;
+        int b = find_bucket(S, lo, hi, key, home);
         unsigned active = __activemask();
         unsigned peers = __match_any_sync(active, b);
         int leader = __ffs(peers) - 1;
@@ -327,14 +331,14 @@ int bucket_sort_perm(nsg_ctx *c)
     const int64_t n = c->n;
     const int src = c->cur;
     const int B = kBucketTarget, cap = kBucketCap;
-    const int nb = (int)((n + B - 1) / B);
+    const int nb = (int)c->nb_total;
     cudaStream_t s = c->stream;
     cudaError_t e = cudaMemsetAsync(c->bcnt, 0, (size_t)nb * 4, s);
     if (e != cudaSuccess) return cuda_err(c, e, "bucket count reset");
     {
         ProfScope ps(c, "bucket_scatter", (double)n * (8 + 4 + 16));
-        k_bucket_scatter<<<grid_for(c, n, 256, 8), 256, 0, s>>>(c->r[src], c->id[src], n, c->split, nb, B,
-                                                                 cap, c->bcnt, c->bkey, c->bpay, c->ctr);
+        k_bucket_scatter<<<grid_for(c, n, 256, 8), 256, 0, s>>>(c->r[src], c->id[src], n, c->split, seg_table(c),
+                                                                 B, cap, c->bcnt, c->bkey, c->bpay, c->ctr);
         k_bucket_scan<<<1, 1024, 0, s>>>(c->bcnt, nb, cap, c->boff, c->ctr);
     }
     {

@@ -57,6 +57,7 @@ struct StepArgs {
     double *q_r, *q_v;          // their fine N=1 result (the coarse pass of level 1)
     uint32_t *lc_idx;
     const int8_t *pred;         // learned schedule: predicted level per position, or null
+    Seg seg;                    // halos of an ensemble (ranks and sizes are per halo)
     // Substep sizes of each pass, identical for every particle, computed once on
     // the host with the same IEEE divisions as nsphere.c:1566-1577 (exact here:
     // h divided by powers of two): coarse N=1 halfKick h/2, midStep h;
@@ -107,15 +108,15 @@ __device__ __forceinline__ void select_out(int out_type, double rc, double vc, d
 }
 
 // Routing of nsphere.c:5804-5822 (alpha rule), or a fixed radius.
-__device__ __forceinline__ bool route_lc(const StepArgs &a, int64_t i, double r, double ell)
+__device__ __forceinline__ bool route_lc(const StepArgs &a, const Local &L, double r, double ell)
 {
     if (a.method != NSG_METHOD_ADAPTIVE_LC || a.lc_rule == NSG_LC_OFF) return false;
     if (a.lc_rule == NSG_LC_RADIUS) return (r > 1.0e-30) && (r < a.lc_radius);
     double r_crit = 0.0;
     if (fabs(ell) > 1.0e-30) {
         double M_enc;
-        if (i == 0) M_enc = dmul(dmul(0.1, ddiv(1.0, (double)a.n)), a.M);
-        else M_enc = dmul(ddiv((double)i, (double)a.n), a.M);
+        if (L.i == 0) M_enc = dmul(dmul(0.1, ddiv(1.0, (double)L.n)), a.M);
+        else M_enc = dmul(ddiv((double)L.i, (double)L.n), a.M);
         double gravPart = dmul(a.G, M_enc);
         r_crit = ddiv(dmul(dmul(ell, ell), a.lc_alpha), gravPart);
     }
@@ -142,9 +143,10 @@ __global__ void __launch_bounds__(256) k_gather_level0(StepArgs a)
         a.id_out[i] = idv;
         if (AUX) a.aux_out[i] = a.aux_src[s];
         a.inv[idv] = (int32_t)i;
-        write_splitter(a.split, i, r);
-        if (route_lc(a, i, r, ell)) continue;
-        const double gn = gnum_of(i, a.n, a.G, a.M, Mpt);
+        const Local L = local_of(a.seg, i, a.n);
+        write_splitter(a.split, a.seg, L, r);
+        if (route_lc(a, L, r, ell)) continue;
+        const double gn = gnum_of(L.i, L.n, a.G, a.M, Mpt);
         const double l2 = dmul(ell, ell);
         const double af = acc_leap(r, gn, l2);
         // learned schedule: a particle predicted to need level >= 1 goes straight to
@@ -225,7 +227,8 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
             v_in = a.v_out[i];
             const double ell = a.ell_out[i];
             l2 = dmul(ell, ell);
-            gn = gnum_of<true>(i, a.n, a.G, a.M, Mpt);
+            const Local L = local_of(a.seg, i, a.n);
+            gn = gnum_of<true>(L.i, L.n, a.G, a.M, Mpt);
             af = a.a0[i];
             rq = a.q_r[e];
             vq = a.q_v[e];
@@ -284,7 +287,7 @@ __global__ void __launch_bounds__(256) k_lc_select(StepArgs a)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t s = a.perm[i];
-        const bool lc = route_lc(a, i, a.r_src[s], a.l_src[s]);
+        const bool lc = route_lc(a, local_of(a.seg, i, a.n), a.r_src[s], a.l_src[s]);
         const int slot = warp_append(lc, &a.ctr->lc_count);
         if (lc) a.lc_idx[slot] = (uint32_t)i;
     }
@@ -314,7 +317,8 @@ __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
         const uint32_t i = a.lc_idx[e];
         const uint32_t s = a.perm[i];
         const double r_in = a.r_src[s], v_in = a.v_src[s], ell = a.l_src[s];
-        const double gn = gnum_of<true>(i, a.n, a.G, a.M, Mpt);
+        const Local L = local_of(a.seg, i, a.n);
+        const double gn = gnum_of<true>(L.i, L.n, a.G, a.M, Mpt);
         int lvmax = 0;
         double ro = r_in, vo = v_in;
         if (!(r_in < 1.0e-30)) {
@@ -468,6 +472,7 @@ static StepArgs make_args(nsg_ctx *c)
     a.q_idx = c->q_idx[0]; a.q_r = c->q_r[0]; a.q_v = c->q_v[0];
     a.lc_idx = c->lc_idx;
     a.pred = nullptr;
+    a.seg = seg_table(c);
     return a;
 }
 

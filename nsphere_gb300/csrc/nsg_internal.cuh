@@ -80,8 +80,17 @@ struct nsg_ctx {
     uint32_t *digit_tot = nullptr;   // [256]
     uint32_t *perm = nullptr;        // result of sort_perm: source index per sorted position
 
+    // ensemble of halos (one segment for a single halo)
+    int nseg = 1;
+    std::vector<int64_t> h_seg_start;   // [nseg + 1]
+    int64_t *d_seg_start = nullptr;
+    int32_t *d_bbase = nullptr;         // [nseg + 1] first bucket of each halo
+    int64_t nb_total = 0;               // buckets over all halos
+    int64_t nb_cap = 0;
+    double *seg_energy = nullptr;       // [2 * nseg] K, W per halo
+
     // near-sorted bucket sort (nsg_bucket.cu)
-    uint64_t *split = nullptr;       // [nb] splitter keys from the last sort
+    uint64_t *split = nullptr;       // [nb_total] splitter keys from the last sort
     bool split_valid = false;
     unsigned int *bcnt = nullptr, *boff = nullptr;  // [nb]
     uint64_t *bkey = nullptr, *bpay = nullptr;      // [nb * kBucketCap]
@@ -158,11 +167,47 @@ __device__ __forceinline__ uint64_t radius_key(double r)
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
-// Splitter of the next near-sorted sort: key(r) at sorted positions b*kBucketTarget,
-// written by the passes that consume a sort (from the sorted start-of-step radii).
-__device__ __forceinline__ void write_splitter(uint64_t *S, int64_t i, double r)
+// Segment table of an ensemble of independent halos: halo h occupies the positions
+// [start[h], start[h+1]) in every copy of the state and is sorted and integrated on
+// its own (its rank and particle count enter the force, nsphere.c:513).  A single
+// halo is the one-segment case.  bbase[h] is the first near-sorted bucket of halo h.
+struct Seg {
+    const int64_t *start;   // [nseg + 1]
+    const int32_t *bbase;   // [nseg + 1]
+    int nseg;
+};
+
+struct Local {
+    int64_t i, n;   // rank within the halo, halo size
+    int h;          // halo
+};
+
+__device__ __forceinline__ int seg_of(const Seg &s, int64_t p)
 {
-    if ((i & (kBucketTarget - 1)) == 0) S[i / kBucketTarget] = (i == 0) ? 0ull : radius_key(r);
+    if (s.nseg <= 1) return 0;
+    int lo = 0, hi = s.nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s.start[mid] <= p) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ Local local_of(const Seg &s, int64_t p, int64_t n_total)
+{
+    if (s.nseg <= 1) return Local{p, n_total, 0};
+    const int h = seg_of(s, p);
+    const int64_t st = s.start[h];
+    return Local{p - st, s.start[h + 1] - st, h};
+}
+
+// Splitter of the next near-sorted sort: key(r) at every kBucketTarget-th sorted
+// position of each halo, written by the passes that consume a sort (from the sorted
+// start-of-step radii); the first splitter of a halo is the smallest key.
+__device__ __forceinline__ void write_splitter(uint64_t *S, const Seg &sg, const Local &L, double r)
+{
+    if ((L.i & (kBucketTarget - 1)) == 0)
+        S[sg.bbase[L.h] + L.i / kBucketTarget] = (L.i == 0) ? 0ull : radius_key(r);
 }
 
 __device__ __forceinline__ unsigned lanemask_lt()
@@ -211,6 +256,7 @@ int integrate_adaptive(nsg_ctx *c);                   // method 3 / 5: sort_perm
 int kdk_first_half(nsg_ctx *c);                       // kick (a0 of the current rank) + drift
 int compute_energy(nsg_ctx *c);                       // K, W of the sorted live copy
 int bucket_sort_perm(nsg_ctx *c);                     // near-sorted fast path (sets need_fallback)
+inline Seg seg_table(const nsg_ctx *c) { return Seg{c->d_seg_start, c->d_bbase, c->nseg}; }
 int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred);  // predicted level per sorted position
 int mlp_features_sorted(nsg_ctx *c);                  // features of the sort (training set)
 int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)

@@ -210,6 +210,7 @@ struct MlpStepArgs {
     int64_t n;
     double G, M, dt;
     const DevCounters *ctr;
+    Seg seg;
 };
 
 // Features of every sorted position (FP32), or predictions (argmax class), from the
@@ -229,7 +230,8 @@ __global__ void __launch_bounds__(256) k_mlp_features(MlpStepArgs s, MlpDev m)
         float f[4] = {0.f, 0.f, 0.f, 0.f};
         if (i < s.n) {
             const uint32_t src = s.perm[i];
-            const double gn = gnum_of(i, s.n, s.G, s.M, Mpt);
+            const Local L = local_of(s.seg, i, s.n);
+            const double gn = gnum_of(L.i, L.n, s.G, s.M, Mpt);
             mlp_features(s.r_src[src], s.v_src[src], s.l_src[src], gn, s.dt, f);
             if (!PREDICT)
                 for (int q = 0; q < 4; q++) m.feat[i * 4 + q] = f[q];
@@ -645,6 +647,7 @@ static MlpStepArgs step_args(nsg_ctx *c)
     s.r_src = c->r[src]; s.v_src = c->vr[src]; s.l_src = c->ell[src];
     s.n = c->n; s.G = c->p.G; s.M = c->p.M_total; s.dt = c->p.dt;
     s.ctr = c->ctr;
+    s.seg = seg_table(c);
     return s;
 }
 

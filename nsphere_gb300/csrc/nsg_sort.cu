@@ -36,10 +36,19 @@ __global__ void k_seed_keys(const double *__restrict__ r, const int32_t *__restr
     if (nan_seen) atomicOr(&ctr->status, NSG_ST_NAN);
 }
 
+// Digit of one pass: 8 key bits at `shift` >= 0, or for shift = -1, -2 the low / high
+// byte of the halo of the element's source position (the passes that group an
+// ensemble by halo after the key passes).
+__device__ __forceinline__ unsigned radix_digit(uint64_t key, uint32_t val, int shift, const Seg &sg)
+{
+    if (shift >= 0) return (unsigned)(key >> shift) & (kRadixBuckets - 1);
+    return ((unsigned)seg_of(sg, val) >> ((-shift - 1) * 8)) & (kRadixBuckets - 1);
+}
+
 // Per-tile histogram of one digit.  counts is digit-major: counts[d * ntiles + t].
 __global__ void __launch_bounds__(kRadixThreads)
-k_tile_hist(const uint64_t *__restrict__ keys, int64_t n, int shift, int ntiles,
-            uint32_t *__restrict__ counts, const DevCounters *__restrict__ ctr)
+k_tile_hist(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ vals, int64_t n, int shift,
+            int ntiles, uint32_t *__restrict__ counts, const DevCounters *__restrict__ ctr, Seg sg)
 {
     if (!ctr->need_fallback) return;
     __shared__ uint32_t h[kRadixBuckets];
@@ -49,7 +58,7 @@ k_tile_hist(const uint64_t *__restrict__ keys, int64_t n, int shift, int ntiles,
 #pragma unroll 4
     for (int j = 0; j < kRadixItems; j++) {
         int64_t idx = base + j * kRadixThreads + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(unsigned)(keys[idx] >> shift) & (kRadixBuckets - 1)], 1u);
+        if (idx < n) atomicAdd(&h[radix_digit(keys[idx], vals[idx], shift, sg)], 1u);
     }
     __syncthreads();
     for (int d = threadIdx.x; d < kRadixBuckets; d += blockDim.x)
@@ -143,7 +152,7 @@ __global__ void __launch_bounds__(kRadixThreads)
 k_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
           uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n,
           int shift, int ntiles, const uint32_t *__restrict__ offsets,
-          const DevCounters *__restrict__ ctr)
+          const DevCounters *__restrict__ ctr, Seg sg)
 {
     if (!ctr->need_fallback) return;
     constexpr int W = kRadixThreads / 32;
@@ -164,7 +173,7 @@ k_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ val
         bool ok = idx < n;
         k[j] = ok ? keys_in[idx] : 0ull;
         v[j] = ok ? vals_in[idx] : 0u;
-        dig[j] = ok ? ((unsigned)(k[j] >> shift) & (kRadixBuckets - 1)) : (unsigned)kRadixBuckets;
+        dig[j] = ok ? radix_digit(k[j], v[j], shift, sg) : (unsigned)kRadixBuckets;
     }
 #pragma unroll
     for (int j = 0; j < kRadixItems; j++) {
@@ -200,10 +209,11 @@ k_scatter(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ val
 }
 
 // Gathers the state into sorted order and computes, per sorted position p, the
-// acceleration at the step start a0 = gnum_p/r^2 + ell^2/r^3 with the force
-// numerator of rank p (nsphere.c:502-535) and the inverse map (nsphere.c:5789-5794).
-// KICK applies the second half-kick of the fixed-step body with the new rank,
-// v += 0.5*a0*dt (nsphere.c:5520-5531), in the same pass.
+// acceleration at the step start a0 = gnum/r^2 + ell^2/r^3 with the force numerator
+// of the particle's rank within its halo (nsphere.c:502-535), the inverse map
+// (nsphere.c:5789-5794) and the next sort's splitters.  KICK applies the second
+// half-kick of the fixed-step body with the new rank, v += 0.5*a0*dt
+// (nsphere.c:5520-5531), in the same pass.
 template <bool AUX, bool KICK>
 __global__ void __launch_bounds__(256)
 k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
@@ -213,15 +223,16 @@ k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
                     double *__restrict__ r1, double *__restrict__ v1, double *__restrict__ l1,
                     int32_t *__restrict__ id1, double *__restrict__ x1,
                     double *__restrict__ a0, int32_t *__restrict__ inv, uint64_t *__restrict__ split,
-                    double G, double M, double dt, const DevCounters *__restrict__ ctr)
+                    double G, double M, double dt, const DevCounters *__restrict__ ctr, Seg sg)
 {
     const double Mpt = ctr->point_mass;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
          p += (int64_t)gridDim.x * blockDim.x) {
+        const Local L = local_of(sg, p, n);
         uint32_t s = perm[p];
         double r = r0[s], v = v0[s], l = l0[s];
         int32_t idv = id0[s];
-        double gn = gnum_of(p, n, G, M, Mpt);
+        double gn = gnum_of(L.i, L.n, G, M, Mpt);
         double acc = acc_leap(r, gn, dmul(l, l));
         if (KICK) v = dadd(v, dmul(dmul(0.5, acc), dt));
         r1[p] = r;
@@ -231,70 +242,96 @@ k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
         if (AUX) x1[p] = x0[s];
         inv[idv] = (int32_t)p;
         a0[p] = acc;
-        write_splitter(split, p, r);
+        write_splitter(split, sg, L, r);
     }
 }
 
-// Energy partial sums of a sorted state: K = sum 1/2 m (v^2 + ell^2/r^2),
+__device__ __forceinline__ void energy_terms(double rr, double vv, double ll, const Local &L, double G,
+                                             double M, double Mpt, double &ek, double &ew)
+{
+    const double m = M / (double)L.n;
+    const double gn = gnum_of(L.i, L.n, G, M, Mpt);
+    ek += 0.5 * m * (vv * vv + (ll * ll) / (rr * rr));
+    ew += m * gn / rr;
+}
+
+// Block sum of two doubles in a fixed tree order; thread 0 gets the result.
+__device__ __forceinline__ void block_sum2(double &a, double &b)
+{
+    __shared__ double sk[32], sw[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { sk[w] = a; sw[w] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0.0, y = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) { x += sk[i]; y += sw[i]; }
+        a = x;
+        b = y;
+    }
+}
+
+// Energy partial sums of a sorted single halo: K = sum 1/2 m (v^2 + ell^2/r^2),
 // W = sum m gnum_i / r_i.  Fixed grid and tree order: deterministic.
 __global__ void __launch_bounds__(256)
 k_energy(const double *__restrict__ r, const double *__restrict__ v, const double *__restrict__ l,
          int64_t n, double G, double M, const DevCounters *__restrict__ ctr, double *__restrict__ red_part)
 {
     const double Mpt = ctr->point_mass;
-    const double m = M / (double)n;
     double ek = 0.0, ew = 0.0;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-         p += (int64_t)gridDim.x * blockDim.x) {
-        double rr = r[p], vv = v[p], ll = l[p];
-        double gn = gnum_of(p, n, G, M, Mpt);
-        ek += 0.5 * m * (vv * vv + (ll * ll) / (rr * rr));
-        ew += m * gn / rr;
-    }
-    __shared__ double sk[8], sw[8];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        ek += __shfl_down_sync(0xffffffffu, ek, o);
-        ew += __shfl_down_sync(0xffffffffu, ew, o);
-    }
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) { sk[w] = ek; sw[w] = ew; }
-    __syncthreads();
+         p += (int64_t)gridDim.x * blockDim.x)
+        energy_terms(r[p], v[p], l[p], Local{p, n, 0}, G, M, Mpt, ek, ew);
+    block_sum2(ek, ew);
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) { a += sk[i]; b += sw[i]; }
-        red_part[blockIdx.x] = a;
-        red_part[kReduceBlocks + blockIdx.x] = b;
+        red_part[blockIdx.x] = ek;
+        red_part[kReduceBlocks + blockIdx.x] = ew;
     }
 }
 
-__global__ void k_finalize_energy(const double *__restrict__ red_part, int nblk, DevCounters *ctr)
+// Energies of an ensemble: one block per halo, deterministic order.
+__global__ void __launch_bounds__(256)
+k_energy_seg(const double *__restrict__ r, const double *__restrict__ v, const double *__restrict__ l,
+             int64_t n, double G, double M, const DevCounters *__restrict__ ctr, Seg sg,
+             double *__restrict__ seg_energy)
 {
-    __shared__ double sk[32], sw[32];
-    double a = 0.0, b = 0.0;
-    for (int i = threadIdx.x; i < nblk; i += blockDim.x) { a += red_part[i]; b += red_part[kReduceBlocks + i]; }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
-    }
-    if ((threadIdx.x & 31) == 0) { sk[threadIdx.x >> 5] = a; sw[threadIdx.x >> 5] = b; }
-    __syncthreads();
+    const double Mpt = ctr->point_mass;
+    const int h = blockIdx.x;
+    const int64_t st = sg.start[h], nh = sg.start[h + 1] - st;
+    double ek = 0.0, ew = 0.0;
+    for (int64_t q = threadIdx.x; q < nh; q += blockDim.x)
+        energy_terms(r[st + q], v[st + q], l[st + q], Local{q, nh, h}, G, M, Mpt, ek, ew);
+    block_sum2(ek, ew);
     if (threadIdx.x == 0) {
-        double x = 0.0, y = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) { x += sk[i]; y += sw[i]; }
-        ctr->energy[0] = x;
-        ctr->energy[1] = y;
+        seg_energy[2 * h] = ek;
+        seg_energy[2 * h + 1] = ew;
     }
 }
 
-// Radix sort of the live copy by (r, id); leaves the permutation in c->perm.
+__global__ void k_finalize_energy(const double *__restrict__ kpart, const double *__restrict__ wpart,
+                                  int nblk, int stride, DevCounters *ctr)
+{
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < nblk; i += blockDim.x) { a += kpart[i * stride]; b += wpart[i * stride]; }
+    block_sum2(a, b);
+    if (threadIdx.x == 0) {
+        ctr->energy[0] = a;
+        ctr->energy[1] = b;
+    }
+}
+
+// Sorts the live copy by (halo, r, id); leaves the permutation in c->perm.
 int sort_perm(nsg_ctx *c)
 {
     const int64_t n = c->n;
     const int src = c->cur;
     const int ntiles = (int)((n + kRadixTile - 1) / kRadixTile);
     cudaStream_t s = c->stream;
+    const Seg sg = seg_table(c);
     // near-sorted fast path when the array is in the order of a previous sort;
     // the radix kernels below run only if it overflowed (or it was not used)
     if (c->split_valid && c->p.sort_mode == 0) {
@@ -309,23 +346,27 @@ int sort_perm(nsg_ctx *c)
         k_seed_keys<<<grid_for(c, n, 256), 256, 0, s>>>(c->r[src], c->id[src], n, c->keys[0],
                                                          c->vals[0], c->ctr);
     }
+    // 8 passes over the radius key, then (ensembles) 2 stable passes over the halo
+    // index; an even pass count leaves the permutation in vals[0], where the bucket
+    // path writes it too
+    const int npass = 8 + (c->nseg > 1 ? 2 : 0);
     int kb = 0;
     {
-        ProfScope ps(c, "sort_radix", (double)n * 8 * (8 + 12 + 12));
-        for (int pass = 0; pass < 8; pass++) {
-            int shift = pass * kRadixBits;
-            k_tile_hist<<<ntiles, kRadixThreads, 0, s>>>(c->keys[kb], n, shift, ntiles, c->tile_counts,
-                                                         c->ctr);
+        ProfScope ps(c, "sort_radix", (double)n * npass * (8 + 12 + 12));
+        for (int pass = 0; pass < npass; pass++) {
+            const int shift = pass < 8 ? pass * kRadixBits : -(pass - 8 + 1);
+            k_tile_hist<<<ntiles, kRadixThreads, 0, s>>>(c->keys[kb], c->vals[kb], n, shift, ntiles,
+                                                         c->tile_counts, c->ctr, sg);
             k_digit_totals<<<kRadixBuckets, 1024, 0, s>>>(c->tile_counts, ntiles, c->digit_tot, c->ctr);
             k_digit_scan<<<kRadixBuckets, 1024, 0, s>>>(c->tile_counts, ntiles, c->digit_tot, c->ctr);
             k_scatter<<<ntiles, kRadixThreads, 0, s>>>(c->keys[kb], c->vals[kb], c->keys[1 - kb],
                                                        c->vals[1 - kb], n, shift, ntiles,
-                                                       c->tile_counts, c->ctr);
+                                                       c->tile_counts, c->ctr, sg);
             kb = 1 - kb;
         }
     }
     c->perm = c->vals[kb];
-    c->launches += 1 + 8 * 4;
+    c->launches += 1 + npass * 4;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "sort kernels");
 }
@@ -335,6 +376,7 @@ static int gather(nsg_ctx *c, bool kick)
     const int64_t n = c->n;
     const int src = c->cur, dst = 1 - c->cur;
     cudaStream_t s = c->stream;
+    const Seg sg = seg_table(c);
     ProfScope ps(c, kick ? "gather_kick" : "rank_force",
                  (double)n * (4 + 28 + 28 + 8 + 4 + (c->p.carry_aux ? 16 : 0)));
     const int grid = grid_for(c, n, 256, 8);
@@ -342,7 +384,7 @@ static int gather(nsg_ctx *c, bool kick)
     k_gather_rank_force<AUXV, KICKV><<<grid, 256, 0, s>>>(                                        \
         c->perm, n, c->r[src], c->vr[src], c->ell[src], c->id[src], c->aux[src], c->r[dst],      \
         c->vr[dst], c->ell[dst], c->id[dst], c->aux[dst], c->a0, c->inv, c->split, c->p.G,       \
-        c->p.M_total, c->p.dt, c->ctr)
+        c->p.M_total, c->p.dt, c->ctr, sg)
     if (c->p.carry_aux) { if (kick) NSG_GATHER(true, true); else NSG_GATHER(true, false); }
     else { if (kick) NSG_GATHER(false, true); else NSG_GATHER(false, false); }
 #undef NSG_GATHER
@@ -371,9 +413,16 @@ int sort_state_kick(nsg_ctx *c)
 int compute_energy(nsg_ctx *c)
 {
     const int s = c->cur;
-    k_energy<<<kReduceBlocks, 256, 0, c->stream>>>(c->r[s], c->vr[s], c->ell[s], c->n, c->p.G,
-                                                   c->p.M_total, c->ctr, c->red_part);
-    k_finalize_energy<<<1, 1024, 0, c->stream>>>(c->red_part, kReduceBlocks, c->ctr);
+    if (c->nseg <= 1) {
+        k_energy<<<kReduceBlocks, 256, 0, c->stream>>>(c->r[s], c->vr[s], c->ell[s], c->n, c->p.G,
+                                                       c->p.M_total, c->ctr, c->red_part);
+        k_finalize_energy<<<1, 1024, 0, c->stream>>>(c->red_part, c->red_part + kReduceBlocks,
+                                                     kReduceBlocks, 1, c->ctr);
+    } else {
+        k_energy_seg<<<c->nseg, 256, 0, c->stream>>>(c->r[s], c->vr[s], c->ell[s], c->n, c->p.G, c->p.M_total,
+                                                      c->ctr, seg_table(c), c->seg_energy);
+        k_finalize_energy<<<1, 1024, 0, c->stream>>>(c->seg_energy, c->seg_energy + 1, c->nseg, 2, c->ctr);
+    }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "energy kernels");
 }

@@ -44,6 +44,21 @@ def plummer(n: int, seed: int = 1):
     return _finish(r, v, mu)
 
 
+def plummer_ensemble(nhalo: int, nmin: int = 10_000, nmax: int = 1_000_000, seed: int = 3):
+    """Independent Plummer halos with N drawn log-uniform in [nmin, nmax] (seeded).
+
+    Returns (r, vr, ell, ids, halo_n): the halos' rows concatenated, each halo in
+    radial order, ids = row index (so halo h owns the ids of its own row range)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = np.floor(10.0 ** rng.uniform(np.log10(nmin), np.log10(nmax), nhalo)).astype(np.int64)
+    parts = [plummer(int(nh), seed=seed * 100003 + h) for h, nh in enumerate(sizes)]
+    r = np.concatenate([p[0] for p in parts])
+    vr = np.concatenate([p[1] for p in parts])
+    ell = np.concatenate([p[2] for p in parts])
+    ids = np.arange(r.shape[0], dtype=np.int32)
+    return r, vr, ell, ids, sizes
+
+
 def hernquist_df(eps):
     """Isotropic Hernquist f(E) for binding energy eps = -E in (0, 1), G = M = a = 1."""
     q = np.sqrt(np.clip(eps, 0.0, 1.0 - 1e-15))

@@ -74,7 +74,7 @@ typedef struct nsg_params {
     int32_t sched;         /* NSG_SCHED_* */
     int32_t carry_aux;     /* 1: permute a fifth float64 column (mu) with the state */
     int32_t sort_mode;     /* 0 auto (near-sorted bucket sort, radix fallback), 1 always radix */
-    int32_t reserved0;
+    int32_t graph;         /* 1: repeat steps by replaying a captured CUDA graph of two steps (default) */
     double point_mass;     /* central point mass added to M_i at the step start (0 = reference) */
     double point_mass_rate;/* d(point_mass)/dt, applied per step (linear ramp) */
 } nsg_params;
@@ -219,6 +219,18 @@ int nsg_counters(nsg_ctx *ctx, int64_t *launches, int64_t *steps);
 
 int nsg_profile(nsg_ctx *ctx, int enable);
 int nsg_profile_read(nsg_ctx *ctx, nsg_kernel_stat *stats, int max, int *count);
+
+/* Launch-shape tuning (no counterpart in the reference, whose step runs on CPU
+ * threads).  vals[4] = {gather_level0 threads (128|256|512), gather_level0 blocks
+ * per SM (1..64), log2 of sorted positions per bucket (8..12), level-kernel blocks
+ * per SM (1..64)}.  Shapes change no arithmetic: results are identical for every
+ * setting. */
+int nsg_tune_get(nsg_ctx *ctx, int32_t *vals, int count);
+int nsg_tune_set(nsg_ctx *ctx, const int32_t *vals, int count);
+/* Times candidate shapes over `steps` steps of the resident state, one knob at a
+ * time, keeps the fastest and restores the state, step count and status exactly.
+ * A JSON summary of the timings is written to report (may be NULL). */
+int nsg_autotune(nsg_ctx *ctx, int steps, char *report, int report_cap);
 
 #ifdef __cplusplus
 }

@@ -34,6 +34,7 @@ EXPORTS = [
     "nsg_upload_ensemble", "nsg_num_halos", "nsg_energy_halos",
     "nsg_mlp_num_params", "nsg_mlp_init", "nsg_mlp_set_weights", "nsg_mlp_get_weights",
     "nsg_mlp_collect", "nsg_mlp_dataset", "nsg_mlp_train", "nsg_mlp_grad", "nsg_mlp_predict",
+    "nsg_tune_get", "nsg_tune_set", "nsg_autotune",
 ]
 
 
@@ -45,7 +46,7 @@ class Params(C.Structure):
         ("out_type", C.c_int32), ("N_taumin", C.c_int32), ("method", C.c_int32),
         ("lc_rule", C.c_int32), ("lc_alpha", C.c_double), ("lc_radius", C.c_double),
         ("max_tau_steps", C.c_int64), ("sched", C.c_int32), ("carry_aux", C.c_int32),
-        ("sort_mode", C.c_int32), ("reserved0", C.c_int32), ("point_mass", C.c_double),
+        ("sort_mode", C.c_int32), ("graph", C.c_int32), ("point_mass", C.c_double),
         ("point_mass_rate", C.c_double),
     ]
 
@@ -105,6 +106,9 @@ def lib() -> C.CDLL:
         "nsg_mlp_grad": [P, P, P, I64, P, P, C.POINTER(D)],
         "nsg_mlp_predict": [P, P, I64, P, P],
         "nsg_profile_read": [P, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)],
+        "nsg_tune_get": [P, P, C.c_int],
+        "nsg_tune_set": [P, P, C.c_int],
+        "nsg_autotune": [P, C.c_int, C.c_char_p, C.c_int],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -311,6 +315,24 @@ class Context:
 
     def profile(self, enable: bool = True):
         self._check(self._L.nsg_profile(self._h, 1 if enable else 0))
+
+    def tune_get(self):
+        """Launch shapes: (gather_level0 threads, its blocks/SM, log2 bucket, level blocks/SM)."""
+        v = (C.c_int32 * 4)()
+        self._check(self._L.nsg_tune_get(self._h, v, 4))
+        return tuple(v)
+
+    def tune_set(self, vals):
+        v = (C.c_int32 * 4)(*[int(x) for x in vals])
+        self._check(self._L.nsg_tune_set(self._h, v, 4))
+
+    def autotune(self, steps=2):
+        """Times candidate launch shapes on the resident state (which it restores) and
+        keeps the fastest; returns the timing report as a dict."""
+        import json
+        buf = C.create_string_buffer(4096)
+        self._check(self._L.nsg_autotune(self._h, int(steps), buf, 4096))
+        return json.loads(buf.value.decode())
 
     def profile_read(self):
         arr = (KernelStat * 64)()

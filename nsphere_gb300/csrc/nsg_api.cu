@@ -81,6 +81,13 @@ void prof_flush(nsg_ctx *c)
     c->stats.swap(merged);
 }
 
+void drop_graph(nsg_ctx *c)
+{
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    c->g_failed = false;
+}
+
 // --------------------------------------------------------- small kernels
 
 __global__ void k_ids_from_double(const double *__restrict__ src, int32_t *__restrict__ dst,
@@ -321,6 +328,7 @@ int nsg_params_default(nsg_params *p)
     p->sched = NSG_SCHED_PLAIN;
     p->carry_aux = 0;
     p->sort_mode = 0;
+    p->graph = 1;
     return NSG_OK;
 }
 
@@ -371,6 +379,7 @@ void nsg_destroy(nsg_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->side) cudaStreamSynchronize(c->side);
     for (auto ev : c->ev_pool) cudaEventDestroy(ev);
+    drop_graph(c);
     free_buffers(c);
     mlp_free(c);
     if (c->ctr) cudaFree(c->ctr);
@@ -396,6 +405,7 @@ int nsg_set_params(nsg_ctx *c, const nsg_params *p)
         return set_err(c, NSG_ESTATE, "carry_aux cannot change while a state is resident");
     bool pm_changed = (p->point_mass != c->p.point_mass);
     c->p = *p;
+    drop_graph(c);
     if (pm_changed) {
         cudaError_t e = cudaMemcpyAsync(&c->ctr->point_mass, &c->p.point_mass, sizeof(double),
                                         cudaMemcpyHostToDevice, c->stream);
@@ -446,7 +456,8 @@ static int setup_segments(nsg_ctx *c, const int64_t *seg_n, int nseg)
     for (int h = 0; h < nseg; h++) {
         if (seg_n[h] <= 0) return set_err(c, NSG_EINVAL, "every halo needs at least one particle");
         start[h + 1] = start[h] + seg_n[h];
-        bbase[h + 1] = bbase[h] + (int32_t)((seg_n[h] + kBucketTarget - 1) / kBucketTarget);
+        const int64_t bt = (int64_t)1 << c->tune.bshift;
+        bbase[h + 1] = bbase[h] + (int32_t)((seg_n[h] + bt - 1) / bt);
     }
     if (start[nseg] != c->n) return set_err(c, NSG_EINVAL, "halo sizes must add up to n");
     const int64_t nb = bbase[nseg];
@@ -479,6 +490,7 @@ static int upload_common(nsg_ctx *c, int64_t n, const int64_t *seg_n = nullptr, 
 {
     if (n <= 0 || n > (int64_t)0x7fffffff) return set_err(c, NSG_EINVAL, "n must be in [1, 2^31-1]");
     if (nseg < 1 || nseg > 65536) return set_err(c, NSG_EINVAL, "1 to 65536 halos");
+    drop_graph(c);
     if (int rc = ensure_capacity(c, n)) return rc;
     c->n = n;
     const int64_t one = n;
@@ -589,29 +601,84 @@ int nsg_sort(nsg_ctx *c)
     return sort_state(c);
 }
 
+// One step of params.method: the reference's time-loop body (nsphere.c:5775-5838 for
+// method 5, :5484-5531 for method 2).
+static int one_step(nsg_ctx *c)
+{
+    int rc = NSG_OK;
+    if (c->p.method == NSG_METHOD_KDK) {
+        // the reference sorts once before its time loop (nsphere.c:5339-5342)
+        if (!c->sorted) rc = sort_state(c);
+        if (!rc) rc = kdk_first_half(c);
+        if (!rc) rc = sort_state_kick(c);
+    } else {
+        rc = integrate_adaptive(c);
+    }
+    if (rc) return rc;
+    if (c->p.point_mass_rate != 0.0) {
+        k_advance_point_mass<<<1, 1, 0, c->stream>>>(c->ctr, c->p.point_mass_rate * c->p.dt);
+        c->launches += 1;
+        c->p.point_mass += c->p.point_mass_rate * c->p.dt;
+        c->sorted = false;
+    }
+    c->steps_done++;
+    return NSG_OK;
+}
+
+// Captures two consecutive steps into a CUDA graph (the eager launch sequence,
+// including the side-stream fork and join) and runs them once.  Returns NSG_OK
+// with c->gexec set, or leaves the graph unset when capture is not possible.
+static int capture_two_steps(nsg_ctx *c)
+{
+    const int64_t l0 = c->launches;
+    const bool sorted0 = c->sorted;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) { cudaGetLastError(); c->g_failed = true; return NSG_OK; }
+    int rc = one_step(c);
+    if (!rc) rc = one_step(c);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(c->stream, &g);
+    if (rc || e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        c->g_failed = true;
+        return rc ? rc : set_err(c, NSG_ECUDA, std::string("step graph capture: ") + cudaGetErrorString(e));
+    }
+    e = cudaGraphInstantiate(&c->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { c->gexec = nullptr; return cuda_err(c, e, "step graph instantiate"); }
+    c->g_launches = c->launches - l0;
+    c->g_sorted = sorted0;
+    e = cudaGraphLaunch(c->gexec, c->stream);
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "step graph launch");
+}
+
 int nsg_step(nsg_ctx *c, int nsteps)
 {
     if (int rc = check_ctx(c)) return rc;
     if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
     if (nsteps < 0) return set_err(c, NSG_EINVAL, "nsteps must be >= 0");
-    for (int j = 0; j < nsteps; j++) {
-        int rc = NSG_OK;
-        if (c->p.method == NSG_METHOD_KDK) {
-            // the reference sorts once before its time loop (nsphere.c:5339-5342)
-            if (!c->sorted) rc = sort_state(c);
-            if (!rc) rc = kdk_first_half(c);
-            if (!rc) rc = sort_state_kick(c);
-        } else {
-            rc = integrate_adaptive(c);
+    for (int j = 0; j < nsteps;) {
+        // steady state: the buffers are in the parity, sort mode and sortedness a
+        // captured pair of steps starts from -> replay it
+        const bool graphable = c->p.graph && !c->g_failed && !c->profiling && !c->mlp_collect &&
+                               nsteps - j >= 2 && c->split_valid && c->cur == 0;
+        if (graphable && c->gexec && c->sorted == c->g_sorted) {
+            cudaError_t e = cudaGraphLaunch(c->gexec, c->stream);
+            if (e != cudaSuccess) return cuda_err(c, e, "step graph launch");
+            c->launches += c->g_launches;
+            c->steps_done += 2;
+            c->p.point_mass += 2 * c->p.point_mass_rate * c->p.dt;
+            if (c->p.point_mass_rate != 0.0) c->sorted = false;
+            j += 2;
+            continue;
         }
-        if (rc) return rc;
-        if (c->p.point_mass_rate != 0.0) {
-            k_advance_point_mass<<<1, 1, 0, c->stream>>>(c->ctr, c->p.point_mass_rate * c->p.dt);
-            c->launches += 1;
-            c->p.point_mass += c->p.point_mass_rate * c->p.dt;
-            c->sorted = false;
+        if (graphable && !c->gexec) {
+            if (int rc = capture_two_steps(c)) return rc;
+            if (c->gexec) { j += 2; continue; }
         }
-        c->steps_done++;
+        if (int rc = one_step(c)) return rc;
+        j++;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(c, e, "step launch");
@@ -861,3 +928,8 @@ int nsg_profile_read(nsg_ctx *c, nsg_kernel_stat *stats, int max, int *count)
 }
 
 }  // extern "C"
+
+int nsg::set_halos(nsg_ctx *c, const int64_t *seg_n, int nseg)
+{
+    return setup_segments(c, seg_n, nseg);
+}

@@ -330,7 +330,7 @@ int bucket_sort_perm(nsg_ctx *c)
 {
     const int64_t n = c->n;
     const int src = c->cur;
-    const int B = kBucketTarget, cap = kBucketCap;
+    const int B = 1 << c->tune.bshift, cap = kBucketCap;
     const int nb = (int)c->nb_total;
     cudaStream_t s = c->stream;
     cudaError_t e = cudaMemsetAsync(c->bcnt, 0, (size_t)nb * 4, s);

@@ -130,7 +130,7 @@ __device__ __forceinline__ bool route_lc(const StepArgs &a, const Local &L, doub
 // acceleration (nsphere.c:502-535) and run adaptive level 0.  The pass is
 // FP64-bound, so the gather traffic hides under the arithmetic.
 template <bool AUX>
-__global__ void __launch_bounds__(256) k_gather_level0(StepArgs a)
+__global__ void __launch_bounds__(512) k_gather_level0(StepArgs a)
 {
     const double Mpt = a.ctr->point_mass;
     const bool last = (a.nlev <= 1);
@@ -509,17 +509,17 @@ int integrate_adaptive(nsg_ctx *c)
     {
         // algorithmic bytes: perm 4, gather r v ell id 28, write r v ell id 28, inv 4, level 1
         ProfScope ps(c, "gather_level0", (double)c->n * (4 + 28 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)));
-        const int grid = grid_for(c, c->n, 256, 8);
-        if (c->p.carry_aux) k_gather_level0<true><<<grid, 256, 0, s>>>(a);
-        else k_gather_level0<false><<<grid, 256, 0, s>>>(a);
+        const int th = c->tune.gl0_threads, grid = grid_for(c, c->n, th, c->tune.gl0_bps);
+        if (c->p.carry_aux) k_gather_level0<true><<<grid, th, 0, s>>>(a);
+        else k_gather_level0<false><<<grid, th, 0, s>>>(a);
         c->launches += 1;
     }
     if (a.nlev > 1) {
         ProfScope ps(c, "leap_levels", 0.0);
         int G = 1;
         while (G < (learned ? a.nlev + 1 : a.nlev - 1)) G <<= 1;
-        if (learned) k_levels_lanes<true><<<c->num_sms * 4, 256, 0, s>>>(a, G);
-        else k_levels_lanes<false><<<c->num_sms * 4, 256, 0, s>>>(a, G);
+        if (learned) k_levels_lanes<true><<<c->num_sms * c->tune.lanes_bps, 256, 0, s>>>(a, G);
+        else k_levels_lanes<false><<<c->num_sms * c->tune.lanes_bps, 256, 0, s>>>(a, G);
         c->launches += 1;
     }
     if (lc) {

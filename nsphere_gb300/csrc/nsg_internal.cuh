@@ -21,8 +21,15 @@ constexpr int kRadixThreads = 256;
 constexpr int kRadixItems = 16;       // keys per thread per tile
 constexpr int kRadixTile = kRadixThreads * kRadixItems;
 constexpr int kReduceBlocks = 1024;   // fixed block count of energy partial sums
-constexpr int kBucketTarget = 2048;   // near-sorted sort: sorted positions per splitter (power of 2)
 constexpr int kBucketCap = 6144;      // entries one bucket block sorts (512 threads x 12)
+
+// Launch shapes chosen by the autotuner (nsg_tune.cu); defaults measured on GB300.
+struct Tune {
+    int gl0_threads = 256;   // k_gather_level0 block size
+    int gl0_bps = 8;         // k_gather_level0 blocks per SM
+    int bshift = 11;         // near-sorted sort: 2^bshift sorted positions per splitter
+    int lanes_bps = 4;       // k_levels_lanes blocks per SM
+};
 
 // Device-resident counters and flags of one context (a single allocation).
 struct DevCounters {
@@ -80,6 +87,8 @@ struct nsg_ctx {
     uint32_t *digit_tot = nullptr;   // [256]
     uint32_t *perm = nullptr;        // result of sort_perm: source index per sorted position
 
+    nsg::Tune tune;
+
     // ensemble of halos (one segment for a single halo)
     int nseg = 1;
     std::vector<int64_t> h_seg_start;   // [nseg + 1]
@@ -110,6 +119,12 @@ struct nsg_ctx {
     // learned level scheduler (nsg_mlp.cu)
     nsg::MlpDev *mlp = nullptr;
     bool mlp_collect = false;        // record (features, level) of each step
+
+    // CUDA graph of two consecutive steps, captured from the stream and replayed
+    cudaGraphExec_t gexec = nullptr;
+    int64_t g_launches = 0;          // kernels in one replay
+    bool g_sorted = false;           // host state the graph was captured from
+    bool g_failed = false;           // capture not possible here: launch eagerly
 
     bool profiling = false;
     std::vector<nsg::KernelStat> stats;
@@ -175,6 +190,7 @@ struct Seg {
     const int64_t *start;   // [nseg + 1]
     const int32_t *bbase;   // [nseg + 1]
     int nseg;
+    int bshift;             // log2 of the sorted positions per splitter (bucket target)
 };
 
 struct Local {
@@ -201,13 +217,13 @@ __device__ __forceinline__ Local local_of(const Seg &s, int64_t p, int64_t n_tot
     return Local{p - st, s.start[h + 1] - st, h};
 }
 
-// Splitter of the next near-sorted sort: key(r) at every kBucketTarget-th sorted
+// Splitter of the next near-sorted sort: key(r) at every 2^bshift-th sorted
 // position of each halo, written by the passes that consume a sort (from the sorted
 // start-of-step radii); the first splitter of a halo is the smallest key.
 __device__ __forceinline__ void write_splitter(uint64_t *S, const Seg &sg, const Local &L, double r)
 {
-    if ((L.i & (kBucketTarget - 1)) == 0)
-        S[sg.bbase[L.h] + L.i / kBucketTarget] = (L.i == 0) ? 0ull : radius_key(r);
+    if ((L.i & ((1ll << sg.bshift) - 1)) == 0)
+        S[sg.bbase[L.h] + (L.i >> sg.bshift)] = (L.i == 0) ? 0ull : radius_key(r);
 }
 
 __device__ __forceinline__ unsigned lanemask_lt()
@@ -256,7 +272,9 @@ int integrate_adaptive(nsg_ctx *c);                   // method 3 / 5: sort_perm
 int kdk_first_half(nsg_ctx *c);                       // kick (a0 of the current rank) + drift
 int compute_energy(nsg_ctx *c);                       // K, W of the sorted live copy
 int bucket_sort_perm(nsg_ctx *c);                     // near-sorted fast path (sets need_fallback)
-inline Seg seg_table(const nsg_ctx *c) { return Seg{c->d_seg_start, c->d_bbase, c->nseg}; }
+inline Seg seg_table(const nsg_ctx *c) { return Seg{c->d_seg_start, c->d_bbase, c->nseg, c->tune.bshift}; }
+void drop_graph(nsg_ctx *c);                          // forget the captured step graph
+int set_halos(nsg_ctx *c, const int64_t *seg_n, int nseg);  // halo table + bucket layout
 int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred);  // predicted level per sorted position
 int mlp_features_sorted(nsg_ctx *c);                  // features of the sort (training set)
 int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)

@@ -150,6 +150,18 @@ int nsg_device_state(nsg_ctx *ctx, double **d_r, double **d_vr, double **d_ell,
  * downloads them permuted.  Uses ctx's buffers and stream. */
 int nsg_sort_particles(nsg_ctx *ctx, double *const *particles, int64_t npts);
 
+/* Allocation-free variant of the sort (no counterpart in the reference, whose sort
+ * runs on host arrays): sorts caller-owned DEVICE columns in place by (r, id) --
+ * ties by id, then input position -- with no context and no device allocation,
+ * its scratch being one fixed 34,078,720-byte __device__ array per device.
+ * npts > 1048576 returns NSG_EINVAL untouched; aux may be NULL; work is queued
+ * on `stream` (a cudaStream_t of the current device, NULL = legacy default).  The
+ * first call on a device looks the scratch address up (cudaGetSymbolAddress) and
+ * should come before any stream capture.  Calls that overlap in time on one
+ * device share the scratch and race: keep them on one stream. */
+int nsg_sort_device_noalloc(double *d_r, double *d_vr, double *d_ell, int32_t *d_id, double *d_aux,
+                            int64_t npts, void *stream);
+
 /* Looks up k particles by id -- the inverse_map reads of the tracking code
  * (nsphere.c:5845-5866, 6384-6450).  rank receives the current array index. */
 int nsg_gather(nsg_ctx *ctx, const int32_t *ids, int k, double *r, double *vr,

@@ -34,7 +34,7 @@ EXPORTS = [
     "nsg_upload_ensemble", "nsg_num_halos", "nsg_energy_halos",
     "nsg_mlp_num_params", "nsg_mlp_init", "nsg_mlp_set_weights", "nsg_mlp_get_weights",
     "nsg_mlp_collect", "nsg_mlp_dataset", "nsg_mlp_train", "nsg_mlp_grad", "nsg_mlp_predict",
-    "nsg_tune_get", "nsg_tune_set", "nsg_autotune",
+    "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc",
 ]
 
 
@@ -109,6 +109,7 @@ def lib() -> C.CDLL:
         "nsg_tune_get": [P, P, C.c_int],
         "nsg_tune_set": [P, P, C.c_int],
         "nsg_autotune": [P, C.c_int, C.c_char_p, C.c_int],
+        "nsg_sort_device_noalloc": [P, P, P, P, P, I64, P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

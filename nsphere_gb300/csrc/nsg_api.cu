@@ -195,7 +195,7 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x)
     return x ^ (x >> 31);
 }
 
-// Compares div_rn with the hardware IEEE division on `count` generated operand
+// Compares div_rn and div_rn_lat with the hardware IEEE division on `count` generated operand
 // pairs of eight classes: random normals, few-bit and all-ones mantissas, equal
 // mantissas, exact products, raw bit patterns (zero/subnormal/inf/NaN), and
 // exponents at the edges of the normal range.
@@ -230,6 +230,11 @@ __global__ void k_selftest_div(uint64_t seed, int64_t count, unsigned long long 
         const double zq = div_rn(z, b), zh = div_rn_hw(z, b), zt = __ddiv_rn(z, b);
         same = same && ((__double_as_longlong(zq) == __double_as_longlong(zt)) || (zq != zq && zt != zt));
         same = same && ((__double_as_longlong(zh) == __double_as_longlong(zt)) || (zh != zh && zt != zt));
+        // the latency-oriented division, where it claims its result
+        bool ok_l, ok_z;
+        const double ql = div_rn_lat(a, b, ok_l), zl = div_rn_lat(z, b, ok_z);
+        if (ok_l) same = same && (__double_as_longlong(ql) == __double_as_longlong(t));
+        if (ok_z) same = same && (__double_as_longlong(zl) == __double_as_longlong(zt));
         if (!same && atomicAdd(&out[1], 1ull) == 0) { first[0] = a; first[1] = b; }
     }
     atomicAdd(&out[2], fast);
@@ -355,13 +360,17 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
         e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
         c->own_stream = true;
     }
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    // the Levi-Civita chains bound the step: their stream gets the highest priority
+    int prio_lo = 0, prio_hi = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_hi);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->ctr, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMemset(c->ctr, 0, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_ctr, sizeof(DevCounters));
     if (e == cudaSuccess && bucket_setup(c) != NSG_OK) e = cudaErrorInvalidValue;
+    if (e == cudaSuccess && lc_setup(c) != NSG_OK) e = cudaErrorInvalidValue;
     if (e == cudaSuccess && p->point_mass != 0.0)
         e = cudaMemcpy(&c->ctr->point_mass, &p->point_mass, sizeof(double), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {

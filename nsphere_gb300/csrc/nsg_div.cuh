@@ -137,6 +137,80 @@ NSG_HD bool div_rn_fast(double a, double b, double *out)
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// Latency-oriented division for serial chains (one particle's Levi-Civita
+// substeps).  On GB300 a dependent FP64 operation takes 64 cycles and the FP64
+// division about 590; this routine takes about 220 on the integer and FP32 pipes.
+//
+// Method (digit recurrence with an approximate reciprocal and exact remainders):
+//   A = ma or 2 ma so that A/mb lies in [1, 2);  ys ~ 2^48/mb in single precision
+//   from rcp.approx of the top 24 bits of mb (relative error < 2^-21);
+//   q1 = round(float(A >> 26) ys)            ~ A 2^22 / mb,  r1 = A 2^22 - q1 mb
+//   q2 = round(float(r1 >> 28) 4 ys)         ~ r1 2^22 / mb, r2 = r1 2^22 - q2 mb
+//   q3 = round(float(r2 >> 28) 2^-11 ys)     ~ r2 2^9 / mb,  r3 = r2 2^9 - q3 mb
+//   Q = q1 2^31 + q2 2^9 + q3 satisfies A 2^53 = Q mb + r3 exactly.  Each
+//   remainder is computed modulo 2^64; its true value is below 2^58 in magnitude
+//   (each digit is within a few units of its ideal value), so the modular result
+//   is exact.  |r3| < mb/2, so one step (r3 < 0: Q - 1, r3 + mb) makes Q the floor
+//   and 0 <= r3 < mb the exact remainder: round bit Q & 1, sticky r3 != 0.
+// There are no branches: every operand runs the same instructions, and `ok` says
+// whether the result stands (both operands normal, or a +-0 dividend over a normal
+// divisor, and a normal quotient); otherwise the caller divides in hardware.  A
+// branch to a fallback inside the chain costs more than the division itself, so
+// callers accumulate the flags and redo the whole chain when one is set.
+NSG_HD float div_lat_rcp(int32_t x)
+{
+#if defined(__CUDA_ARCH__)
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(__int2float_rn(x)));
+    return y;
+#elif defined(NSG_DIV_HOST_RCP)
+    return NSG_DIV_HOST_RCP(x);   // host tests substitute perturbed estimates
+#else
+    return 1.0f / (float)x;
+#endif
+}
+
+NSG_HD int32_t div_lat_digit(int32_t top, float scale)
+{
+#if defined(__CUDA_ARCH__)
+    return __float2int_rn(__int2float_rn(top) * scale);
+#else
+    return (int32_t)__builtin_nearbyintf((float)top * scale);
+#endif
+}
+
+NSG_HD double div_rn_lat(double a, double b, bool &ok)
+{
+    const uint64_t ua = div_bits(a), ub = div_bits(b);
+    const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+    const uint64_t sign = (ua ^ ub) & (1ull << 63);
+    const bool bnorm = eb - 1u < 2046u;
+    const bool zero = bnorm && (ua << 1) == 0ull;
+    const uint64_t MANT = (1ull << 52) - 1ull, HID = 1ull << 52;
+    const uint64_t ma = (ua & MANT) | HID, mb = (ub & MANT) | HID;
+    const bool lt = ma < mb;
+    const uint64_t A = lt ? ma << 1 : ma;
+    const int32_t e = (int32_t)ea - (int32_t)eb + 1023 - (lt ? 1 : 0);
+    const float ys = div_lat_rcp((int32_t)(mb >> 29)) * 0x1p19f;
+    const int32_t q1 = div_lat_digit((int32_t)(A >> 26), ys);
+    const int64_t r1 = (int64_t)((A << 22) - (uint64_t)(int64_t)q1 * mb);
+    const int32_t q2 = div_lat_digit((int32_t)(r1 >> 28), ys * 4.0f);
+    const int64_t r2 = (int64_t)(((uint64_t)r1 << 22) - (uint64_t)(int64_t)q2 * mb);
+    const int32_t q3 = div_lat_digit((int32_t)(r2 >> 28), ys * 0x1p-11f);
+    const int64_t r3 = (int64_t)(((uint64_t)r2 << 9) - (uint64_t)(int64_t)q3 * mb);
+    const int64_t Q = ((int64_t)q1 << 31) + ((int64_t)q2 << 9) + (int64_t)q3;
+    const bool neg = r3 < 0;
+    const int64_t rr = neg ? r3 + (int64_t)mb : r3;
+    const uint64_t Qc = (uint64_t)(neg ? Q - 1 : Q);
+    uint64_t m = Qc >> 1;
+    m += (Qc & 1ull) & ((uint64_t)(rr != 0) | (m & 1ull));
+    // m in [2^52, 2^53]; 2^53 carries into the exponent field
+    const uint64_t bits = sign | (((uint64_t)(uint32_t)(e - 1) << 52) + m);
+    ok = zero || ((ea - 1u < 2046u) && bnorm && ((uint32_t)(e - 1) < 2045u) && rr >= 0 && rr < (int64_t)mb);
+    return div_from_bits(zero ? sign : bits);
+}
+
 #if defined(__CUDACC__)
 // Correctly rounded a / b (round to nearest even), bit-identical to __ddiv_rn.
 __device__ __forceinline__ double div_rn(double a, double b)

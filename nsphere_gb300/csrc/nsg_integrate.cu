@@ -293,27 +293,123 @@ __global__ void __launch_bounds__(256) k_lc_select(StepArgs a)
     }
 }
 
-// One warp per Levi-Civita particle (nsphere.c:2231-2334).  Lane roles in each
-// adaptive tau-step (nsphere.c:2077-2186): lane 0 the coarse N=1 pass (3
-// substeps), lane 1+k the fine pass of level k (4*2^k+1 substeps; it is also the
-// coarse pass of level k+1), lane nlev+1 the fallback fine pass at N = 2^nlev.
-// Requires nlev + 2 <= 32 (max_subdiv < 2^30, checked by the host).  Launched
-// with one warp per block.
+// Division in the Levi-Civita chains.  FAST: the latency-oriented division, with
+// `bad` recording whether any quotient must be redone on the FP64 pipe; otherwise
+// the FP64 pipe's division (zero dividends answered directly).
+template <bool FAST>
+__device__ __forceinline__ double lc_div(double a, double b, bool &bad)
+{
+    if (FAST) {
+        bool ok;
+        const double q = div_rn_lat(a, b, ok);
+        bad |= !ok;
+        return q;
+    }
+    return div_rn_hw(a, b);
+}
+
+// Levi-Civita force gnum/(rho*rho) + l2/(rho*rho*rho*rho), nsphere.c:563-599,
+// 1777-1787, with the division above.
+template <bool FAST>
+__device__ __forceinline__ double lc_force(double rho, double gn, double l2, bool &bad)
+{
+    const double p2 = dmul(rho, rho);
+    const double p4 = dmul(dmul(p2, rho), rho);
+    return dadd(lc_div<FAST>(gn, p2, bad), lc_div<FAST>(l2, p4, bad));
+}
+
+struct LcTau {
+    double r, v, t;   // end of the tau-step (rho, v, physical time)
+    int lv;           // accepted level, -1: fallback or non-finite
+};
+
+// One adaptive tau-step from (rho, v, t) (nsphere.c:2077-2186), every lane running
+// its own pass: lane 0 the coarse N=1 pass (3 substeps), lane 1+k the fine pass of
+// level k (4*2^k+1 substeps; it is also the coarse pass of level k+1), lane nlev+1
+// the fallback fine pass at N = 2^nlev.  Level k is decided as soon as its fine pass
+// ends.  The loop is bounded by the fallback pass (fb_sub substeps) whatever the
+// values.  hdt*force is carried from one substep to the next: the reference forms
+// the same product at the end of a substep and at the start of the next.
+template <bool FAST>
+__device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, double v, double t,
+                                             double gn, double l2, double dtau, double hdt,
+                                             int64_t my_sub, int64_t fb_sub, int nlev, bool &bad)
+{
+    double pr = rho, pv = v, pt = t;
+    double hpf = dmul(hdt, lc_force<FAST>(rho, gn, l2, bad));
+    LcTau o{rho, v, t, -2};
+    int kcheck = 0;
+    int64_t next_end = 5;                // substeps after which level kcheck's fine pass ends
+    for (int64_t ss = 0; o.lv == -2; ss++) {
+        if (ss < my_sub) {
+            const double vh = dadd(pv, hpf);
+            const double rnx = dadd(pr, dmul(dtau, dmul(dmul(0.5, pr), vh)));
+            const double hf2 = dmul(hdt, lc_force<FAST>(rnx, gn, l2, bad));
+            const double vnx = dadd(vh, hf2);
+            const double rm = dmul(0.5, dadd(pr, rnx));
+            pt = dadd(pt, dmul(dtau, dmul(rm, rm)));
+            pr = rnx;
+            pv = vnx;
+            hpf = hf2;
+        }
+        if (kcheck < nlev && ss + 1 == next_end) {
+            const int lf = 1 + kcheck, lcz = kcheck;  // fine(k) lane, coarse(k) lane
+            const double rF = __shfl_sync(0xffffffffu, pr, lf);
+            const double vF = __shfl_sync(0xffffffffu, pv, lf);
+            const double tF = __shfl_sync(0xffffffffu, pt, lf);
+            const double rC = __shfl_sync(0xffffffffu, pr, lcz);
+            const double vC = __shfl_sync(0xffffffffu, pv, lcz);
+            const double tC = __shfl_sync(0xffffffffu, pt, lcz);
+            const double rsq = dmul(rF, rF);
+            if (converged<true>(rC, vC, rF, vF, rsq, a.tol_r, a.tol_v)) {
+                if (a.out_type == 0) { o.r = rC; o.v = vC; o.t = tC; }
+                else if (a.out_type == 1) { o.r = rF; o.v = vF; o.t = tF; }
+                else {
+                    double rr = dsub(dmul(4.0, rF), dmul(3.0, rC));
+                    o.v = dsub(dmul(4.0, vF), dmul(3.0, vC));
+                    o.t = dsub(dmul(4.0, tF), dmul(3.0, tC));
+                    if (rr < 0.0) rr = 0.0;
+                    o.r = rr;
+                }
+                o.lv = kcheck;
+            } else if (!(isfinite(rF) && isfinite(vF))) {
+                o.r = rF; o.v = vF; o.t = tF;   // non-finite: stop climbing
+                o.lv = -1;
+            }
+            kcheck++;
+            next_end = 4 * ((int64_t)1 << kcheck) + 1;
+        }
+        if (o.lv == -2 && kcheck >= nlev && ss + 1 == fb_sub) {
+            o.r = __shfl_sync(0xffffffffu, pr, nlev + 1);
+            o.v = __shfl_sync(0xffffffffu, pv, nlev + 1);
+            o.t = __shfl_sync(0xffffffffu, pt, nlev + 1);
+            o.lv = -1;
+        }
+    }
+    return o;
+}
+
+// One warp per Levi-Civita particle (nsphere.c:2231-2334), tau-steps until the
+// physical time passes dt.  Each tau-step runs first with the latency-oriented
+// division; if any lane met an operand that it does not handle, the warp redoes
+// that tau-step from its start with the FP64 pipe's division, so every result is
+// the one the reference computes.  Requires nlev + 2 <= 32 (max_subdiv < 2^30,
+// checked by the host).  Launched with one warp per block and the largest dynamic
+// shared memory a block may take, which it does not use: each block then has an SM
+// to itself, and the chain's FP64 instructions never queue behind other kernels'.
 __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
 {
     const unsigned cnt = a.ctr->lc_count;
     if (cnt == 0) return;
     const double Mpt = a.ctr->point_mass;
     const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int nlev = a.nlev;
     int64_t my_sub = 0;                        // substeps of this lane's pass (0: idle)
     if (lane == 0) my_sub = 3;
     else if (lane <= nlev) my_sub = 4 * ((int64_t)1 << (lane - 1)) + 1;
     else if (lane == nlev + 1) my_sub = 4 * ((int64_t)1 << nlev) + 1;
     const int64_t fb_sub = 4 * ((int64_t)1 << nlev) + 1;
-    for (int64_t e = gw; e < cnt; e += warps) {
+    for (int64_t e = blockIdx.x; e < cnt; e += gridDim.x) {
         const uint32_t i = a.lc_idx[e];
         const uint32_t s = a.perm[i];
         const double r_in = a.r_src[s], v_in = a.v_src[s], ell = a.l_src[s];
@@ -336,72 +432,26 @@ __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
             bool done = false;
             for (;;) {
                 if (t >= a.dt) break;
-                // ---- one adaptive tau-step from (rho, v, t) over hg
-                double pr = rho, pv = v, pt = t, pf = acc_lc<true>(rho, gn, l2);
-                double rn = rho, vn = v, tn = t;
-                int acc_lv = -2;               // accepted level (-1: fallback)
-                int kcheck = 0;
-                int64_t next_end = 5;          // substeps after which level kcheck's fine pass ends
-                for (int64_t ss = 0; acc_lv == -2; ss++) {
-                    if (ss < my_sub) {
-                        const double vh = dadd(pv, dmul(hdt, pf));
-                        const double rnx = dadd(pr, dmul(dtau, dmul(dmul(0.5, pr), vh)));
-                        const double f2 = acc_lc<true>(rnx, gn, l2);
-                        const double vnx = dadd(vh, dmul(hdt, f2));
-                        const double rm = dmul(0.5, dadd(pr, rnx));
-                        pt = dadd(pt, dmul(dtau, dmul(rm, rm)));
-                        pr = rnx;
-                        pv = vnx;
-                        pf = f2;
-                    }
-                    if (kcheck < nlev && ss + 1 == next_end) {
-                        const int lf = 1 + kcheck, lcz = kcheck;  // fine(k) lane, coarse(k) lane
-                        const double rF = __shfl_sync(0xffffffffu, pr, lf);
-                        const double vF = __shfl_sync(0xffffffffu, pv, lf);
-                        const double tF = __shfl_sync(0xffffffffu, pt, lf);
-                        const double rC = __shfl_sync(0xffffffffu, pr, lcz);
-                        const double vC = __shfl_sync(0xffffffffu, pv, lcz);
-                        const double tC = __shfl_sync(0xffffffffu, pt, lcz);
-                        const double rsq = dmul(rF, rF);
-                        if (converged<true>(rC, vC, rF, vF, rsq, a.tol_r, a.tol_v)) {
-                            if (a.out_type == 0) { rn = rC; vn = vC; tn = tC; }
-                            else if (a.out_type == 1) { rn = rF; vn = vF; tn = tF; }
-                            else {
-                                double rr = dsub(dmul(4.0, rF), dmul(3.0, rC));
-                                vn = dsub(dmul(4.0, vF), dmul(3.0, vC));
-                                tn = dsub(dmul(4.0, tF), dmul(3.0, tC));
-                                if (rr < 0.0) rr = 0.0;
-                                rn = rr;
-                            }
-                            acc_lv = kcheck;
-                        } else if (!(isfinite(rF) && isfinite(vF))) {
-                            rn = rF; vn = vF; tn = tF;  // non-finite: stop climbing
-                            acc_lv = -1;
-                        }
-                        kcheck++;
-                        next_end = 4 * ((int64_t)1 << kcheck) + 1;
-                    }
-                    if (acc_lv == -2 && kcheck >= nlev && ss + 1 == fb_sub) {
-                        rn = __shfl_sync(0xffffffffu, pr, nlev + 1);
-                        vn = __shfl_sync(0xffffffffu, pv, nlev + 1);
-                        tn = __shfl_sync(0xffffffffu, pt, nlev + 1);
-                        acc_lv = -1;
-                    }
+                bool bad = false;
+                LcTau o = lc_tau_step<true>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, bad);
+                if (__any_sync(0xffffffffu, bad)) {
+                    bool unused = false;
+                    o = lc_tau_step<false>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, unused);
                 }
-                if (acc_lv < 0) lvmax = -1;
-                else if (lvmax >= 0 && acc_lv > lvmax) lvmax = acc_lv;
+                if (o.lv < 0) lvmax = -1;
+                else if (lvmax >= 0 && o.lv > lvmax) lvmax = o.lv;
                 // ---- physical-time bookkeeping of nsphere.c:2290-2323
-                if (tn > a.dt) {
+                if (o.t > a.dt) {
                     double alpha = 0.0;
-                    if (fabs(dsub(tn, t)) > 1.0e-30) alpha = __ddiv_rn(dsub(a.dt, t), dsub(tn, t));
-                    const double rf = dadd(rho, dmul(alpha, dsub(rn, rho)));
-                    const double vf = dadd(v, dmul(alpha, dsub(vn, v)));
+                    if (fabs(dsub(o.t, t)) > 1.0e-30) alpha = __ddiv_rn(dsub(a.dt, t), dsub(o.t, t));
+                    const double rf = dadd(rho, dmul(alpha, dsub(o.r, rho)));
+                    const double vf = dadd(v, dmul(alpha, dsub(o.v, v)));
                     ro = dmul(rf, rf);
                     vo = vf;
                     done = true;
                     break;
                 }
-                rho = rn; v = vn; t = tn;
+                rho = o.r; v = o.v; t = o.t;
                 steps++;
                 if (steps > a.max_tau_steps || !(isfinite(rho) && isfinite(t))) {
                     if (lane == 0) atomicOr(&a.ctr->status, NSG_ST_TAU_CAP);
@@ -416,6 +466,17 @@ __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
             a.level[i] = (int8_t)(lvmax < 0 ? kLevelLcFallback : kLevelLcBase + lvmax);
         }
     }
+}
+
+int lc_setup(nsg_ctx *c)
+{
+    int dev = 0, smem = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_levi_civita_lanes, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return cuda_err(c, e, "levi-civita kernel setup");
+    c->lc_smem = smem;
+    return NSG_OK;
 }
 
 // ------------------------------------------------------------ fixed-step KDK
@@ -492,17 +553,23 @@ int integrate_adaptive(nsg_ctx *c)
     if (e != cudaSuccess) return cuda_err(c, e, "memset queue counters");
     const bool lc = (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF);
     if (lc) {
-        // Levi-Civita particles start on the side stream as soon as the order is known
+        // Levi-Civita particles start on the side stream (the highest-priority
+        // stream) as soon as they are selected, before the main stream's kernels
+        {
+            ProfScope ps(c, "lc_select", (double)c->n * 20);
+            k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, s>>>(a);
+            c->launches += 1;
+        }
         e = cudaEventRecord(c->ev_fork, s);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
         if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
         ProfScope ps(c, "levi_civita", 0.0, c->side);
-        k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, c->side>>>(a);
-        // one warp per block, so consecutive particles land on different SMs: a
-        // warp-wide FP64 instruction occupies an SM's FP64 pipe for many cycles,
-        // and these chains are latency-bound
-        k_levi_civita_lanes<<<c->num_sms * 4, 32, 0, c->side>>>(a);
-        c->launches += 2;
+        // one warp per block and one block per SM (its shared memory request keeps
+        // other blocks off the SM): a warp-wide FP64 instruction occupies an SM's
+        // FP64 pipe for many cycles, and these chains are latency-bound.  At most
+        // a third of the SMs are taken; further particles wait for a free block.
+        k_levi_civita_lanes<<<c->num_sms / 3, 32, c->lc_smem, c->side>>>(a);
+        c->launches += 1;
         e = cudaEventRecord(c->ev_join, c->side);
         if (e != cudaSuccess) return cuda_err(c, e, "join record");
     }

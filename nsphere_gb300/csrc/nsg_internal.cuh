@@ -62,6 +62,7 @@ struct nsg_ctx {
     bool own_stream = false;
     int device = 0;
     int num_sms = 0;
+    int lc_smem = 0;                 // dynamic shared memory of a Levi-Civita block
     std::string err;
 
     int64_t n = 0, cap = 0;
@@ -141,9 +142,9 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 // Division: throughput-bound kernels divide on the integer/FP32 pipes
-// (div_rn, nsg_div.cuh); latency-bound ones (a few long serial chains) use the
-// FP64 pipe's shorter dependent sequence.  Both are IEEE round-to-nearest, so
-// the choice never changes a result bit.
+// (div_rn, nsg_div.cuh); the Levi-Civita chains use the latency-oriented
+// div_rn_lat with the FP64 pipe's division as its fallback.  All are IEEE
+// round-to-nearest, so the choice never changes a result bit.
 template <bool HW>
 __device__ __forceinline__ double ddivx(double a, double b) { return HW ? div_rn_hw(a, b) : div_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return div_rn(a, b); }
@@ -163,15 +164,6 @@ __device__ __forceinline__ double acc_leap(double r, double gnum, double l2)
 {
     double r2 = dmul(r, r);
     return dadd(ddivx<HW>(gnum, r2), ddivx<HW>(l2, dmul(r2, r)));
-}
-
-// Levi-Civita: gnum/(rho*rho) + l2/(rho*rho*rho*rho), nsphere.c:563-599, 1777-1787.
-template <bool HW = false>
-__device__ __forceinline__ double acc_lc(double rho, double gnum, double l2)
-{
-    double p2 = dmul(rho, rho);
-    double p4 = dmul(dmul(p2, rho), rho);
-    return dadd(ddivx<HW>(gnum, p2), ddivx<HW>(l2, p4));
 }
 
 // Order-preserving map of a double to uint64: -0.0 -> +0.0, NaN -> all ones.
@@ -280,6 +272,7 @@ int mlp_features_sorted(nsg_ctx *c);                  // features of the sort (t
 int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)
 void mlp_free(nsg_ctx *c);
 int bucket_setup(nsg_ctx *c);
+int lc_setup(nsg_ctx *c);            // Levi-Civita kernel attributes
 int launch_gather(nsg_ctx *c, const int32_t *d_ids, int k, double *d_out, int32_t *d_rank);
 int launch_level_hist(nsg_ctx *c);
 int launch_ids_from_double(nsg_ctx *c, const double *d_src, int32_t *d_dst, int64_t n);

@@ -319,9 +319,43 @@ __device__ __forceinline__ double lc_force(double rho, double gn, double l2, boo
 }
 
 struct LcTau {
-    double r, v, t;   // end of the tau-step (rho, v, physical time)
+    double r, v, t;   // end of the tau-step (rho, v, physical time; t only when computed inline)
     int lv;           // accepted level, -1: fallback or non-finite
+    int lc, lf;       // lanes whose times make the end time (-1: not needed)
 };
+
+// Exact x/2 for normal x with a biased exponent above 1; other operands set `bad`.
+__device__ __forceinline__ double lc_half(double x, bool &bad)
+{
+    const uint64_t u = (uint64_t)__double_as_longlong(x);
+    const uint32_t ex = (uint32_t)(u >> 52) & 0x7ffu;
+    bad |= (ex - 2u) >= 2045u;
+    return __longlong_as_double((long long)(u - (1ull << 52)));
+}
+
+// Acceptance test of nsphere.c:2125-2128 with the chain's division.
+template <bool FAST>
+__device__ __forceinline__ bool lc_converged(double rc, double vc, double rf, double vf, double rscale,
+                                             double tol_r, double tol_v, bool &bad)
+{
+    const double dr = lc_div<FAST>(fabs(dsub(rf, rc)), dadd(fabs(rscale), 1.0e-30), bad);
+    const double dv = lc_div<FAST>(fabs(dsub(vf, vc)), dadd(fabs(vf), 1.0e-30), bad);
+    return (dr < tol_r) && (dv < tol_v);
+}
+
+// Slots of each lane's pass in a tau-step record of radii (PAIR form): lane 0 the
+// coarse pass (3 substeps), lane 1+k the fine pass of level k, lane nlev+1 the
+// fallback pass.
+__host__ __device__ __forceinline__ int64_t lc_slot(int lane, int nlev)
+{
+    if (lane == 0) return 0;
+    const int k = lane - 1;                      // 3 + sum_{j<k} (4*2^j + 1)
+    return 3 + 4 * (((int64_t)1 << k) - 1) + k;
+}
+__host__ __device__ __forceinline__ int64_t lc_slots(int nlev)
+{
+    return lc_slot(nlev + 1, nlev) + 4 * ((int64_t)1 << nlev) + 1;
+}
 
 // One adaptive tau-step from (rho, v, t) (nsphere.c:2077-2186), every lane running
 // its own pass: lane 0 the coarse N=1 pass (3 substeps), lane 1+k the fine pass of
@@ -330,50 +364,71 @@ struct LcTau {
 // ends.  The loop is bounded by the fallback pass (fb_sub substeps) whatever the
 // values.  hdt*force is carried from one substep to the next: the reference forms
 // the same product at the end of a substep and at the start of the next.
-template <bool FAST>
+// PAIR: the physical time is left to a companion warp; each lane stores the radius
+// after each of its substeps at xs[ss] (its own slots), and the result names the
+// lanes whose times the end time is made of.  A tau-step run past the particle's
+// end is abandoned at the next level check once `abandon` is set (lv = -3).
+template <bool FAST, bool PAIR>
 __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, double v, double t,
                                              double gn, double l2, double dtau, double hdt,
-                                             int64_t my_sub, int64_t fb_sub, int nlev, bool &bad)
+                                             int64_t my_sub, int64_t fb_sub, int nlev, double *xs,
+                                             const volatile int *abandon, bool &bad)
 {
     double pr = rho, pv = v, pt = t;
     double hpf = dmul(hdt, lc_force<FAST>(rho, gn, l2, bad));
-    LcTau o{rho, v, t, -2};
+    LcTau o{rho, v, t, -2, -1, -1};
     int kcheck = 0;
     int64_t next_end = 5;                // substeps after which level kcheck's fine pass ends
     for (int64_t ss = 0; o.lv == -2; ss++) {
         if (ss < my_sub) {
             const double vh = dadd(pv, hpf);
-            const double rnx = dadd(pr, dmul(dtau, dmul(dmul(0.5, pr), vh)));
+            const double hp = (FAST && PAIR) ? lc_half(pr, bad) : dmul(0.5, pr);
+            const double rnx = dadd(pr, dmul(dtau, dmul(hp, vh)));
             const double hf2 = dmul(hdt, lc_force<FAST>(rnx, gn, l2, bad));
             const double vnx = dadd(vh, hf2);
-            const double rm = dmul(0.5, dadd(pr, rnx));
-            pt = dadd(pt, dmul(dtau, dmul(rm, rm)));
+            if (PAIR) {
+                xs[ss] = rnx;
+            } else {
+                const double rm = dmul(0.5, dadd(pr, rnx));
+                pt = dadd(pt, dmul(dtau, dmul(rm, rm)));
+            }
             pr = rnx;
             pv = vnx;
             hpf = hf2;
         }
         if (kcheck < nlev && ss + 1 == next_end) {
+            if (PAIR) {
+                // the companion warp has ended the particle: this tau-step is not needed
+                const int ab = __shfl_sync(0xffffffffu, (threadIdx.x & 31) == 0 ? *abandon : 0, 0);
+                if (ab) { o.lv = -3; break; }
+            }
             const int lf = 1 + kcheck, lcz = kcheck;  // fine(k) lane, coarse(k) lane
             const double rF = __shfl_sync(0xffffffffu, pr, lf);
             const double vF = __shfl_sync(0xffffffffu, pv, lf);
-            const double tF = __shfl_sync(0xffffffffu, pt, lf);
             const double rC = __shfl_sync(0xffffffffu, pr, lcz);
             const double vC = __shfl_sync(0xffffffffu, pv, lcz);
-            const double tC = __shfl_sync(0xffffffffu, pt, lcz);
+            double tF = 0.0, tC = 0.0;
+            if (!PAIR) {
+                tF = __shfl_sync(0xffffffffu, pt, lf);
+                tC = __shfl_sync(0xffffffffu, pt, lcz);
+            }
             const double rsq = dmul(rF, rF);
-            if (converged<true>(rC, vC, rF, vF, rsq, a.tol_r, a.tol_v)) {
-                if (a.out_type == 0) { o.r = rC; o.v = vC; o.t = tC; }
-                else if (a.out_type == 1) { o.r = rF; o.v = vF; o.t = tF; }
+            if (lc_converged<FAST>(rC, vC, rF, vF, rsq, a.tol_r, a.tol_v, bad)) {
+                if (a.out_type == 0) { o.r = rC; o.v = vC; o.t = tC; o.lc = lcz; }
+                else if (a.out_type == 1) { o.r = rF; o.v = vF; o.t = tF; o.lf = lf; }
                 else {
                     double rr = dsub(dmul(4.0, rF), dmul(3.0, rC));
                     o.v = dsub(dmul(4.0, vF), dmul(3.0, vC));
-                    o.t = dsub(dmul(4.0, tF), dmul(3.0, tC));
+                    if (!PAIR) o.t = dsub(dmul(4.0, tF), dmul(3.0, tC));
                     if (rr < 0.0) rr = 0.0;
                     o.r = rr;
+                    o.lc = lcz;
+                    o.lf = lf;
                 }
                 o.lv = kcheck;
             } else if (!(isfinite(rF) && isfinite(vF))) {
                 o.r = rF; o.v = vF; o.t = tF;   // non-finite: stop climbing
+                o.lf = lf;
                 o.lv = -1;
             }
             kcheck++;
@@ -382,7 +437,8 @@ __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, doub
         if (o.lv == -2 && kcheck >= nlev && ss + 1 == fb_sub) {
             o.r = __shfl_sync(0xffffffffu, pr, nlev + 1);
             o.v = __shfl_sync(0xffffffffu, pv, nlev + 1);
-            o.t = __shfl_sync(0xffffffffu, pt, nlev + 1);
+            if (!PAIR) o.t = __shfl_sync(0xffffffffu, pt, nlev + 1);
+            o.lf = nlev + 1;
             o.lv = -1;
         }
     }
@@ -433,10 +489,10 @@ __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
             for (;;) {
                 if (t >= a.dt) break;
                 bool bad = false;
-                LcTau o = lc_tau_step<true>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, bad);
+                LcTau o = lc_tau_step<true, false>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, nullptr, nullptr, bad);
                 if (__any_sync(0xffffffffu, bad)) {
                     bool unused = false;
-                    o = lc_tau_step<false>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, unused);
+                    o = lc_tau_step<false, false>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, nullptr, nullptr, unused);
                 }
                 if (o.lv < 0) lvmax = -1;
                 else if (lvmax >= 0 && o.lv > lvmax) lvmax = o.lv;
@@ -468,12 +524,211 @@ __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
     }
 }
 
+// Named barriers of the paired kernel (barrier 0 is __syncthreads): FULL(b) after
+// the leading warp wrote tau-step record b, EMPTY(b) after the trailing warp read it.
+__device__ __forceinline__ void lc_bar_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ void lc_bar_arrive(int id) { asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory"); }
+constexpr int kLcFull = 1, kLcEmpty = 3;
+
+struct LcRecord {
+    double r, v;      // end of the tau-step (rho, v)
+    int lv, lc, lf;   // accepted level and the lanes whose times make the end time
+    int pad;
+};
+
+// Shared memory of the paired kernel: two tau-step records, the stop flag, each
+// lane's dtau, then two buffers of lc_slots(nlev) radii.
+__host__ __device__ __forceinline__ size_t lc_pair_smem(int nlev)
+{
+    return 2 * sizeof(LcRecord) + 16 + 32 * sizeof(double) + 2 * (size_t)lc_slots(nlev) * sizeof(double);
+}
+
+// Levi-Civita particles with two warps each (nsphere.c:2231-2334).  A warp cannot
+// overlap its own FP64 instructions on GB300 (each occupies it for the full 64-cycle
+// latency), so the physical-time chain t += dtau (rho_mid)^2, which no decision of
+// the tau-step reads, runs on a second warp.  The leading warp runs tau-steps back
+// to back (lc_tau_step, PAIR form), storing each lane's radii in one of two buffers
+// and publishing a record; the trailing warp replays the time sums of the lanes the
+// record names, in the reference's order, and applies the time bookkeeping of
+// nsphere.c:2290-2323: it decides when the particle is done, interpolates, writes
+// the result and raises the stop flag.  The leading warp reads the flag before each
+// tau-step from the third on, so it runs at most one tau-step past the end.
+// Barrier protocol (count 64 = both warps): for m >= 2 the leader syncs on
+// EMPTY(m&1) before tau-step m (the trailer is done with record m-2, whose buffer
+// it reuses) and arrives at FULL(m&1) after it.  The trailer syncs on FULL(m&1),
+// reads record m (or, once stopped, just consumes it) and arrives at EMPTY(m&1).
+// The leader reads the stop flag after each EMPTY sync; when set, it writes
+// term_at = m, arrives at FULL(m&1) without a record (the termination token) and
+// syncs on EMPTY((m+1)&1) to absorb the trailer's arrival for record m-1; the
+// trailer leaves when the FULL it synced on is the token.  Every barrier phase then
+// has both warps (checked by a model of the two warps over random interleavings),
+// so both leave together, and the leader runs at most one tau-step past the end.
+__global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char lc_sm[];
+    LcRecord *rec = reinterpret_cast<LcRecord *>(lc_sm);
+    volatile int *stop = reinterpret_cast<volatile int *>(lc_sm + 2 * sizeof(LcRecord));
+    volatile long long *term_at = reinterpret_cast<volatile long long *>(lc_sm + 2 * sizeof(LcRecord) + 8);
+    double *dtau_sm = reinterpret_cast<double *>(lc_sm + 2 * sizeof(LcRecord) + 16);
+    double *xbuf = dtau_sm + 32;
+    const unsigned cnt = a.ctr->lc_count;
+    if (cnt == 0) return;
+    const double Mpt = a.ctr->point_mass;
+    const int lane = threadIdx.x & 31;
+    const bool lead = threadIdx.x < 32;
+    const int nlev = a.nlev;
+    const int64_t W = lc_slots(nlev);
+    int64_t my_sub = 0;                        // substeps of this lane's pass (0: idle)
+    if (lane == 0) my_sub = 3;
+    else if (lane <= nlev) my_sub = 4 * ((int64_t)1 << (lane - 1)) + 1;
+    else if (lane == nlev + 1) my_sub = 4 * ((int64_t)1 << nlev) + 1;
+    const int64_t fb_sub = 4 * ((int64_t)1 << nlev) + 1;
+    const int64_t off = my_sub ? lc_slot(lane, nlev) : 0;
+    for (int64_t e = blockIdx.x; e < cnt; e += gridDim.x) {
+        const uint32_t i = a.lc_idx[e];
+        const uint32_t s = a.perm[i];
+        const double r_in = a.r_src[s], v_in = a.v_src[s], ell = a.l_src[s];
+        __syncthreads();                       // the previous particle's buffers are free
+        if (threadIdx.x == 0) { *stop = 0; *term_at = -1; }
+        if (r_in < 1.0e-30) {
+            if (threadIdx.x == 0) {
+                a.r_out[i] = r_in;
+                a.v_out[i] = v_in;
+                a.level[i] = (int8_t)kLevelLcBase;
+            }
+            continue;
+        }
+        const double rho0 = sqrt(r_in);
+        double hg;
+        if (r_in > 1.0e-30 && a.N_taumin > 0)
+            hg = __ddiv_rn(a.dt, dmul(dmul(2.0, r_in), (double)a.N_taumin));
+        else
+            hg = __ddiv_rn(a.dt, 100.0);
+        const double dtau = my_sub ? __ddiv_rn(hg, (double)my_sub) : 0.0;
+        if (lead) dtau_sm[lane] = dtau;
+        __syncthreads();
+        if (lead) {
+            const Local L = local_of(a.seg, i, a.n);
+            const double gn = gnum_of<true>(L.i, L.n, a.G, a.M, Mpt);
+            const double l2 = dmul(ell, ell);
+            const double hdt = dmul(0.5, dtau);
+            double rho = rho0, v = v_in;
+            for (int64_t m = 0;; m++) {
+                const int b = (int)(m & 1);
+                if (m >= 2) {
+                    lc_bar_sync(kLcEmpty + b);
+                    const int st = __shfl_sync(0xffffffffu, lane == 0 ? *stop : 0, 0);
+                    if (st) {
+                        if (lane == 0) *term_at = m;
+                        __threadfence_block();
+                        __syncwarp();
+                        lc_bar_arrive(kLcFull + b);
+                        lc_bar_sync(kLcEmpty + (b ^ 1));
+                        break;
+                    }
+                }
+                double *xs = xbuf + b * W + off;
+                bool bad = false;
+                LcTau o = lc_tau_step<true, true>(a, rho, v, 0.0, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, xs,
+                                                  stop, bad);
+                if (o.lv != -3 && __any_sync(0xffffffffu, bad)) {
+                    bool unused = false;
+                    o = lc_tau_step<false, true>(a, rho, v, 0.0, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, xs,
+                                                 stop, unused);
+                }
+                if (lane == 0) rec[b] = LcRecord{o.r, o.v, o.lv, o.lc, o.lf, 0};
+                __threadfence_block();
+                __syncwarp();
+                lc_bar_arrive(kLcFull + b);
+                rho = o.r;
+                v = o.v;
+            }
+        } else {
+            double rho = rho0, v = v_in, t = 0.0, ro = 0.0, vo = 0.0;
+            int64_t steps = 0;
+            int lvmax = 0;
+            bool stopped = false;
+            for (int64_t m = 0;; m++) {
+                const int b = (int)(m & 1);
+                lc_bar_sync(kLcFull + b);
+                if (*term_at == m) break;      // the leader's termination token
+                if (stopped) {                 // a tau-step run past the end: discarded
+                    lc_bar_arrive(kLcEmpty + b);
+                    continue;
+                }
+                bool fin = false;
+                if (t >= a.dt) {               // nsphere.c:2245: no further tau-step
+                    ro = dmul(rho, rho);
+                    vo = v;
+                    fin = true;
+                } else {
+                    const LcRecord R = rec[b];
+                    // time sums of the named lanes, in the reference's order
+                    const int L = lane == 0 ? R.lc : (lane == 1 ? R.lf : -1);
+                    double pt = t;
+                    if (L >= 0) {
+                        const int64_t ns = (L == 0) ? 3 : 4 * ((int64_t)1 << (L - 1)) + 1;
+                        const double dl = dtau_sm[L];
+                        const double *x = xbuf + b * W + lc_slot(L, nlev);
+                        double pr = rho;
+                        for (int64_t ss = 0; ss < ns; ss++) {
+                            const double rnx = x[ss];
+                            const double rm = dmul(0.5, dadd(pr, rnx));
+                            pt = dadd(pt, dmul(dl, dmul(rm, rm)));
+                            pr = rnx;
+                        }
+                    }
+                    const double tC = __shfl_sync(0xffffffffu, pt, 0);
+                    const double tF = __shfl_sync(0xffffffffu, pt, 1);
+                    double tn;
+                    if (R.lc >= 0 && R.lf >= 0) tn = dsub(dmul(4.0, tF), dmul(3.0, tC));
+                    else if (R.lc >= 0) tn = tC;
+                    else tn = tF;
+                    if (R.lv < 0) lvmax = -1;
+                    else if (lvmax >= 0 && R.lv > lvmax) lvmax = R.lv;
+                    if (tn > a.dt) {
+                        double alpha = 0.0;
+                        if (fabs(dsub(tn, t)) > 1.0e-30) alpha = __ddiv_rn(dsub(a.dt, t), dsub(tn, t));
+                        const double rf = dadd(rho, dmul(alpha, dsub(R.r, rho)));
+                        const double vf = dadd(v, dmul(alpha, dsub(R.v, v)));
+                        ro = dmul(rf, rf);
+                        vo = vf;
+                        fin = true;
+                    } else {
+                        rho = R.r; v = R.v; t = tn;
+                        steps++;
+                        if (steps > a.max_tau_steps || !(isfinite(rho) && isfinite(t))) {
+                            if (lane == 0) atomicOr(&a.ctr->status, NSG_ST_TAU_CAP);
+                            ro = dmul(rho, rho);
+                            vo = v;
+                            fin = true;
+                        }
+                    }
+                }
+                if (fin) {
+                    stopped = true;
+                    if (lane == 0) {
+                        *stop = 1;
+                        a.r_out[i] = ro;
+                        a.v_out[i] = vo;
+                        a.level[i] = (int8_t)(lvmax < 0 ? kLevelLcFallback : kLevelLcBase + lvmax);
+                    }
+                }
+                __threadfence_block();
+                __syncwarp();
+                lc_bar_arrive(kLcEmpty + b);
+            }
+        }
+    }
+}
+
 int lc_setup(nsg_ctx *c)
 {
     int dev = 0, smem = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_levi_civita_lanes, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_levi_civita_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return cuda_err(c, e, "levi-civita kernel setup");
     c->lc_smem = smem;
     return NSG_OK;
@@ -568,7 +823,10 @@ int integrate_adaptive(nsg_ctx *c)
         // other blocks off the SM): a warp-wide FP64 instruction occupies an SM's
         // FP64 pipe for many cycles, and these chains are latency-bound.  At most
         // a third of the SMs are taken; further particles wait for a free block.
-        k_levi_civita_lanes<<<c->num_sms / 3, 32, c->lc_smem, c->side>>>(a);
+        if (lc_pair_smem(a.nlev) <= (size_t)c->lc_smem)
+            k_levi_civita_pair<<<c->num_sms / 3, 64, c->lc_smem, c->side>>>(a);
+        else
+            k_levi_civita_lanes<<<c->num_sms / 3, 32, c->lc_smem, c->side>>>(a);
         c->launches += 1;
         e = cudaEventRecord(c->ev_join, c->side);
         if (e != cudaSuccess) return cuda_err(c, e, "join record");

@@ -111,22 +111,24 @@ def _adaptive_case(n, seed, lowl=0):
     return r, vr, ell, ids
 
 
-@pytest.mark.parametrize("lc_rule,lc_radius,dt,msub", [
-    (0, 1e-3, 5e-4, 128),      # reference r_crit rule
-    (1, 1e-1, 5e-4, 128),      # fixed radius rule (many Levi-Civita particles)
-    (0, 1e-3, 5e-3, 1 << 12),  # deeper levels
-    (2, 1e-3, 2e-2, 64),       # leapfrog only, level cap reached
+@pytest.mark.parametrize("lc_rule,lc_radius,dt,msub,out_type", [
+    (0, 1e-3, 5e-4, 128, 2),      # reference r_crit rule
+    (1, 1e-1, 5e-4, 128, 2),      # fixed radius rule (many Levi-Civita particles)
+    (0, 1e-3, 5e-3, 1 << 12, 2),  # deeper levels (single-warp Levi-Civita kernel)
+    (2, 1e-3, 2e-2, 64, 2),       # leapfrog only, level cap reached
+    (1, 3e-2, 5e-4, 128, 0),      # coarse-pass output
+    (1, 3e-2, 5e-4, 128, 1),      # fine-pass output
 ])
-def test_adaptive_step_bit_exact(nsg, oracle, lc_rule, lc_radius, dt, msub):
+def test_adaptive_step_bit_exact(nsg, oracle, lc_rule, lc_radius, dt, msub, out_type):
     n = 20000
     r, vr, ell, ids = _adaptive_case(n, 21, lowl=100)
-    with _ctx(nsg, dt=dt, max_subdiv=msub, lc_rule=lc_rule, lc_radius=lc_radius) as c:
+    with _ctx(nsg, dt=dt, max_subdiv=msub, lc_rule=lc_rule, lc_radius=lc_radius, out_type=out_type) as c:
         c.upload(r, vr, ell, ids)
         c.step(1)
         gr, gv, gl, gid = c.download()
         glv = c.levels()
         hist = c.level_hist(10)
-    p = oracle.params(dt=dt, max_subdiv=msub, lc_rule=lc_rule, lc_radius=lc_radius)
+    p = oracle.params(dt=dt, max_subdiv=msub, lc_rule=lc_rule, lc_radius=lc_radius, out_type=out_type)
     orr, ov, ol, oid, olv, cap = oracle.step_adaptive(p, r, vr, ell, ids)
     assert np.array_equal(gid, oid)
     assert np.array_equal(glv, olv), "accepted levels differ"

@@ -360,10 +360,11 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
         e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
         c->own_stream = true;
     }
-    // the Levi-Civita chains bound the step: their stream gets the highest priority
+    // the leapfrog kernels run on the side stream, at the lowest priority: the
+    // Levi-Civita chains on the main stream bound the step
     int prio_lo = 0, prio_hi = 0;
     if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
-    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->ctr, sizeof(DevCounters));

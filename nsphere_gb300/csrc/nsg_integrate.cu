@@ -309,12 +309,26 @@ __device__ __forceinline__ double lc_div(double a, double b, bool &bad)
 }
 
 // Levi-Civita force gnum/(rho*rho) + l2/(rho*rho*rho*rho), nsphere.c:563-599,
-// 1777-1787, with the division above.
-template <bool FAST>
+// 1777-1787, with the division above.  ZG (a zero gravity numerator, the innermost
+// particle without a central mass): gnum/(rho*rho) is a signed zero and adding it
+// returns l2/rho^4 unchanged, since that quotient is never -0 (l2 >= 0, rho^4 >= 0)
+// and every quotient the fast division accepts is finite.
+// SPLIT (lanes 16-31 mirror lanes 0-15): the lower lane of each pair divides l2 by
+// rho^4 and the upper one gnum by rho^2 in the same instructions, and the quotients
+// are exchanged -- one division's latency instead of two that the warp would issue
+// in turn.  Both lanes then add the same operands in the same order.
+template <bool FAST, bool ZG = false, bool SPLIT = false>
 __device__ __forceinline__ double lc_force(double rho, double gn, double l2, bool &bad)
 {
     const double p2 = dmul(rho, rho);
     const double p4 = dmul(dmul(p2, rho), rho);
+    if (FAST && ZG) return lc_div<FAST>(l2, p4, bad);
+    if (FAST && SPLIT) {
+        const bool hi = (threadIdx.x & 16) != 0;
+        const double q = lc_div<FAST>(hi ? gn : l2, hi ? p2 : p4, bad);
+        const double qo = __shfl_xor_sync(0xffffffffu, q, 16);
+        return hi ? dadd(q, qo) : dadd(qo, q);
+    }
     return dadd(lc_div<FAST>(gn, p2, bad), lc_div<FAST>(l2, p4, bad));
 }
 
@@ -368,34 +382,38 @@ __host__ __device__ __forceinline__ int64_t lc_slots(int nlev)
 // after each of its substeps at xs[ss] (its own slots), and the result names the
 // lanes whose times the end time is made of.  A tau-step run past the particle's
 // end is abandoned at the next level check once `abandon` is set (lv = -3).
-template <bool FAST, bool PAIR>
+template <bool FAST, bool PAIR, bool ZG, typename IT>
 __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, double v, double t,
                                              double gn, double l2, double dtau, double hdt,
-                                             int64_t my_sub, int64_t fb_sub, int nlev, double *xs,
+                                             IT my_sub, IT fb_sub, int nlev, double *xs,
                                              const volatile int *abandon, bool &bad)
 {
     double pr = rho, pv = v, pt = t;
-    double hpf = dmul(hdt, lc_force<FAST>(rho, gn, l2, bad));
+    double hpf = dmul(hdt, lc_force<FAST, ZG, PAIR>(rho, gn, l2, bad));
     LcTau o{rho, v, t, -2, -1, -1};
     int kcheck = 0;
-    int64_t next_end = 5;                // substeps after which level kcheck's fine pass ends
-    for (int64_t ss = 0; o.lv == -2; ss++) {
-        if (ss < my_sub) {
-            const double vh = dadd(pv, hpf);
-            const double hp = (FAST && PAIR) ? lc_half(pr, bad) : dmul(0.5, pr);
-            const double rnx = dadd(pr, dmul(dtau, dmul(hp, vh)));
-            const double hf2 = dmul(hdt, lc_force<FAST>(rnx, gn, l2, bad));
-            const double vnx = dadd(vh, hf2);
-            if (PAIR) {
-                xs[ss] = rnx;
-            } else {
-                const double rm = dmul(0.5, dadd(pr, rnx));
-                pt = dadd(pt, dmul(dtau, dmul(rm, rm)));
-            }
-            pr = rnx;
-            pv = vnx;
-            hpf = hf2;
+    IT next_end = 5;                     // substeps after which level kcheck's fine pass ends
+    for (IT ss = 0; o.lv == -2; ss++) {
+        // every lane computes (the warp issues each instruction once whatever the
+        // active lanes); a lane whose pass has ended keeps its state
+        const bool act = ss < my_sub;
+        bool bs = false;
+        const double vh = dadd(pv, hpf);
+        const double hp = (FAST && PAIR) ? lc_half(pr, bs) : dmul(0.5, pr);
+        const double rnx = dadd(pr, dmul(dtau, dmul(hp, vh)));
+        const double hf2 = dmul(hdt, lc_force<FAST, ZG, PAIR>(rnx, gn, l2, bs));
+        const double vnx = dadd(vh, hf2);
+        if (PAIR) {
+            if (act && (threadIdx.x & 16) == 0) xs[ss] = rnx;
+        } else {
+            const double rm = dmul(0.5, dadd(pr, rnx));
+            const double ptn = dadd(pt, dmul(dtau, dmul(rm, rm)));
+            pt = act ? ptn : pt;
         }
+        pr = act ? rnx : pr;
+        pv = act ? vnx : pv;
+        hpf = act ? hf2 : hpf;
+        bad |= act && bs;
         if (kcheck < nlev && ss + 1 == next_end) {
             if (PAIR) {
                 // the companion warp has ended the particle: this tau-step is not needed
@@ -489,10 +507,12 @@ __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
             for (;;) {
                 if (t >= a.dt) break;
                 bool bad = false;
-                LcTau o = lc_tau_step<true, false>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, nullptr, nullptr, bad);
+                LcTau o = lc_tau_step<true, false, false, int64_t>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev,
+                                                                   nullptr, nullptr, bad);
                 if (__any_sync(0xffffffffu, bad)) {
                     bool unused = false;
-                    o = lc_tau_step<false, false>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, nullptr, nullptr, unused);
+                    o = lc_tau_step<false, false, false, int64_t>(a, rho, v, t, gn, l2, dtau, hdt, my_sub, fb_sub, nlev,
+                                                              nullptr, nullptr, unused);
                 }
                 if (o.lv < 0) lvmax = -1;
                 else if (lvmax >= 0 && o.lv > lvmax) lvmax = o.lv;
@@ -543,7 +563,8 @@ __host__ __device__ __forceinline__ size_t lc_pair_smem(int nlev)
     return 2 * sizeof(LcRecord) + 16 + 32 * sizeof(double) + 2 * (size_t)lc_slots(nlev) * sizeof(double);
 }
 
-// Levi-Civita particles with two warps each (nsphere.c:2231-2334).  A warp cannot
+// Levi-Civita particles with two warps each (nsphere.c:2231-2334); needs nlev + 2
+// <= 16 (lanes 16-31 of the leading warp mirror lanes 0-15 for the split force).  A warp cannot
 // overlap its own FP64 instructions on GB300 (each occupies it for the full 64-cycle
 // latency), so the physical-time chain t += dtau (rho_mid)^2, which no decision of
 // the tau-step reads, runs on a second warp.  The leading warp runs tau-steps back
@@ -575,15 +596,16 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
     if (cnt == 0) return;
     const double Mpt = a.ctr->point_mass;
     const int lane = threadIdx.x & 31;
+    const int role = lane & 15;                // leading warp: lanes 16-31 mirror lanes 0-15
     const bool lead = threadIdx.x < 32;
     const int nlev = a.nlev;
     const int64_t W = lc_slots(nlev);
     int64_t my_sub = 0;                        // substeps of this lane's pass (0: idle)
-    if (lane == 0) my_sub = 3;
-    else if (lane <= nlev) my_sub = 4 * ((int64_t)1 << (lane - 1)) + 1;
-    else if (lane == nlev + 1) my_sub = 4 * ((int64_t)1 << nlev) + 1;
+    if (role == 0) my_sub = 3;
+    else if (role <= nlev) my_sub = 4 * ((int64_t)1 << (role - 1)) + 1;
+    else if (role == nlev + 1) my_sub = 4 * ((int64_t)1 << nlev) + 1;
     const int64_t fb_sub = 4 * ((int64_t)1 << nlev) + 1;
-    const int64_t off = my_sub ? lc_slot(lane, nlev) : 0;
+    const int64_t off = my_sub ? lc_slot(role, nlev) : 0;
     for (int64_t e = blockIdx.x; e < cnt; e += gridDim.x) {
         const uint32_t i = a.lc_idx[e];
         const uint32_t s = a.perm[i];
@@ -605,13 +627,15 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
         else
             hg = __ddiv_rn(a.dt, 100.0);
         const double dtau = my_sub ? __ddiv_rn(hg, (double)my_sub) : 0.0;
-        if (lead) dtau_sm[lane] = dtau;
+        if (lead && lane < 16) dtau_sm[lane] = dtau;
         __syncthreads();
         if (lead) {
             const Local L = local_of(a.seg, i, a.n);
             const double gn = gnum_of<true>(L.i, L.n, a.G, a.M, Mpt);
             const double l2 = dmul(ell, ell);
             const double hdt = dmul(0.5, dtau);
+            const bool zg = (gn == 0.0);
+            const int sub32 = (int)my_sub, fb32 = (int)fb_sub;   // nlev <= 10 here
             double rho = rho0, v = v_in;
             for (int64_t m = 0;; m++) {
                 const int b = (int)(m & 1);
@@ -629,12 +653,14 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
                 }
                 double *xs = xbuf + b * W + off;
                 bool bad = false;
-                LcTau o = lc_tau_step<true, true>(a, rho, v, 0.0, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, xs,
-                                                  stop, bad);
+                LcTau o = zg ? lc_tau_step<true, true, true, int>(a, rho, v, 0.0, gn, l2, dtau, hdt, sub32, fb32,
+                                                                  nlev, xs, stop, bad)
+                             : lc_tau_step<true, true, false, int>(a, rho, v, 0.0, gn, l2, dtau, hdt, sub32, fb32,
+                                                                   nlev, xs, stop, bad);
                 if (o.lv != -3 && __any_sync(0xffffffffu, bad)) {
                     bool unused = false;
-                    o = lc_tau_step<false, true>(a, rho, v, 0.0, gn, l2, dtau, hdt, my_sub, fb_sub, nlev, xs,
-                                                 stop, unused);
+                    o = lc_tau_step<false, true, false, int>(a, rho, v, 0.0, gn, l2, dtau, hdt, sub32, fb32, nlev,
+                                                             xs, stop, unused);
                 }
                 if (lane == 0) rec[b] = LcRecord{o.r, o.v, o.lv, o.lc, o.lf, 0};
                 __threadfence_block();
@@ -807,9 +833,12 @@ int integrate_adaptive(nsg_ctx *c)
     e = cudaMemsetAsync(&c->ctr->lc_count, 0, sizeof(unsigned) * (kMaxLevels + 2), s);
     if (e != cudaSuccess) return cuda_err(c, e, "memset queue counters");
     const bool lc = (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF);
+    // With Levi-Civita particles, their kernel follows the selection directly on the
+    // main stream and the leapfrog kernels run on the side stream after a
+    // cross-stream wait, which resolves later: the Levi-Civita blocks, each of which
+    // needs a whole SM, are placed before the leapfrog blocks fill the GPU.
+    cudaStream_t ls = s;
     if (lc) {
-        // Levi-Civita particles start on the side stream (the highest-priority
-        // stream) as soon as they are selected, before the main stream's kernels
         {
             ProfScope ps(c, "lc_select", (double)c->n * 20);
             k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, s>>>(a);
@@ -818,38 +847,38 @@ int integrate_adaptive(nsg_ctx *c)
         e = cudaEventRecord(c->ev_fork, s);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
         if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
-        ProfScope ps(c, "levi_civita", 0.0, c->side);
-        // one warp per block and one block per SM (its shared memory request keeps
-        // other blocks off the SM): a warp-wide FP64 instruction occupies an SM's
-        // FP64 pipe for many cycles, and these chains are latency-bound.  At most
-        // a third of the SMs are taken; further particles wait for a free block.
-        if (lc_pair_smem(a.nlev) <= (size_t)c->lc_smem)
-            k_levi_civita_pair<<<c->num_sms / 3, 64, c->lc_smem, c->side>>>(a);
+        ls = c->side;
+        ProfScope ps(c, "levi_civita", 0.0);
+        // one block per SM (its shared memory request keeps other blocks off the
+        // SM): a warp cannot overlap its own FP64 instructions, and another kernel's
+        // warps on the SM would queue on the same FP64 pipe.  At most a third of the
+        // SMs are taken; further particles wait for a free block.
+        if (a.nlev + 2 <= 16 && lc_pair_smem(a.nlev) <= (size_t)c->lc_smem)
+            k_levi_civita_pair<<<c->num_sms / 3, 64, c->lc_smem, s>>>(a);
         else
-            k_levi_civita_lanes<<<c->num_sms / 3, 32, c->lc_smem, c->side>>>(a);
+            k_levi_civita_lanes<<<c->num_sms / 3, 32, c->lc_smem, s>>>(a);
         c->launches += 1;
-        e = cudaEventRecord(c->ev_join, c->side);
-        if (e != cudaSuccess) return cuda_err(c, e, "join record");
     }
     {
         // algorithmic bytes: perm 4, gather r v ell id 28, write r v ell id 28, inv 4, level 1
-        ProfScope ps(c, "gather_level0", (double)c->n * (4 + 28 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)));
+        ProfScope ps(c, "gather_level0", (double)c->n * (4 + 28 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)), ls);
         const int th = c->tune.gl0_threads, grid = grid_for(c, c->n, th, c->tune.gl0_bps);
-        if (c->p.carry_aux) k_gather_level0<true><<<grid, th, 0, s>>>(a);
-        else k_gather_level0<false><<<grid, th, 0, s>>>(a);
+        if (c->p.carry_aux) k_gather_level0<true><<<grid, th, 0, ls>>>(a);
+        else k_gather_level0<false><<<grid, th, 0, ls>>>(a);
         c->launches += 1;
     }
     if (a.nlev > 1) {
-        ProfScope ps(c, "leap_levels", 0.0);
+        ProfScope ps(c, "leap_levels", 0.0, ls);
         int G = 1;
         while (G < (learned ? a.nlev + 1 : a.nlev - 1)) G <<= 1;
-        if (learned) k_levels_lanes<true><<<c->num_sms * c->tune.lanes_bps, 256, 0, s>>>(a, G);
-        else k_levels_lanes<false><<<c->num_sms * c->tune.lanes_bps, 256, 0, s>>>(a, G);
+        if (learned) k_levels_lanes<true><<<c->num_sms * c->tune.lanes_bps, 256, 0, ls>>>(a, G);
+        else k_levels_lanes<false><<<c->num_sms * c->tune.lanes_bps, 256, 0, ls>>>(a, G);
         c->launches += 1;
     }
     if (lc) {
-        e = cudaStreamWaitEvent(s, c->ev_join, 0);
-        if (e != cudaSuccess) return cuda_err(c, e, "join wait");
+        e = cudaEventRecord(c->ev_join, c->side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_join, 0);
+        if (e != cudaSuccess) return cuda_err(c, e, "join");
     }
     if (c->mlp_collect)
         if (int rc = mlp_append_levels(c)) return rc;

@@ -57,7 +57,7 @@ struct KernelStat {
 struct nsg_ctx {
     nsg_params p{};
     cudaStream_t stream = nullptr;
-    cudaStream_t side = nullptr;     // Levi-Civita work runs here, overlapped
+    cudaStream_t side = nullptr;     // leapfrog kernels beside the Levi-Civita chains
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool own_stream = false;
     int device = 0;

@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--workload", choices=["adaptive", "kdk"], default="adaptive")
     ap.add_argument("--sched", choices=["plain", "learned"], default="plain")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--ab-steps", type=int, default=8, help="steps of the learned/plain comparison (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
@@ -228,6 +229,7 @@ def main():
     r, vr, ell, ids = state
     n = len(r)
     fp64 = ns.probe_fp64()
+    fp64["latency_cycles"] = ns.probe_latency()
 
     # a dedicated (non-default) stream shared by the library and the timing events
     stream = torch.cuda.Stream()
@@ -282,6 +284,40 @@ def main():
     kprof = ctx.profile_read()
     ctx.profile(False)
     ctx.set_params(p)
+
+    # learned against plain schedule on the same state: collect levels from plain steps,
+    # train on the GPU, then time the same steps under each schedule from one snapshot.
+    # Both schedules give bit-identical states, so |dE/E| is equal by construction.
+    learned = None
+    if args.workload == "adaptive" and args.ab_steps > 0:
+        ctx.mlp_init(4)
+        ctx.mlp_collect(3, keep_level0=0.02, capacity=1 << 21)
+        loss = ctx.mlp_train(epochs=4, batch=2048, lr=3e-3, seed=4)
+        snap = ctx.download()
+
+        def timed(sched):
+            q = ns.default_params(**params)
+            q.sched = sched
+            ctx.set_params(q)
+            ctx.upload(*snap)
+            ctx.step(1)
+            barrier()
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            ctx.step(args.ab_steps)
+            t1.record(stream)
+            barrier()
+            return t0.elapsed_time(t1), sum(ctx.energy()), ctx.download()
+
+        ms_l, e_l, s_l = timed(ns.SCHED_LEARNED)
+        ms_p, e_p, s_p = timed(ns.SCHED_PLAIN)
+        same = all(np.array_equal(a_, b_) for a_, b_ in zip(s_l, s_p))
+        learned = {"steps": args.ab_steps, "train_loss": loss,
+                   "learned_value": n * args.ab_steps / (ms_l / 1e3),
+                   "plain_value": n * args.ab_steps / (ms_p / 1e3),
+                   "speedup": ms_p / ms_l, "identical_states": bool(same),
+                   "dE_over_E_learned": abs(e_l - E0) / abs(E0), "dE_over_E_plain": abs(e_p - E0) / abs(E0)}
+        ctx.set_params(p)
 
     # end to end through the public C ABI with host buffers: upload (pinned), step, download
     pin = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(8)]
@@ -363,6 +399,7 @@ def main():
             "energy_drift_steps": args.warmup + args.steps,
             "level_hist": [int(x) for x in hist],
             "status": status,
+            "learned_vs_plain": learned,
         }
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(state, params, args.cpu_seconds)

@@ -199,6 +199,14 @@ int nsg_selftest_division(uint64_t seed, int64_t count, int64_t *mismatches,
  * and one division in cycles. */
 int nsg_probe_fp64(double *dfma_tflops, double *div_hw_gps, double *div_int_gps,
                    double *fma_latency_cycles, double *div_latency_cycles);
+/* Dependent latencies in cycles per iteration, one block on one SM (no reference
+ * counterpart): cycles[0] FP64 FMA chain; [1] two independent FMA chains in one warp;
+ * [2] one chain in each of two warps; [3] dadd + FP64-pipe division; [4] dadd +
+ * integer-pipe division (throughput form); [5] dadd + latency-oriented division;
+ * [6] 32-bit integer multiply-add; [7] 64-bit multiply-high; [8] int->float, multiply,
+ * float->int; [9] one Levi-Civita substep of the leading warp (split force); [10] the
+ * same with a zero gravity numerator.  count = how many to measure (<= 11). */
+int nsg_probe_latency(double *cycles, int count);
 
 /* ---- learned level scheduler (no reference counterpart: an addition of this
  * library).  A 4 -> 64 -> 64 -> 8 MLP with BF16 weights and FP32 accumulation

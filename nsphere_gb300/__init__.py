@@ -34,7 +34,7 @@ EXPORTS = [
     "nsg_upload_ensemble", "nsg_num_halos", "nsg_energy_halos",
     "nsg_mlp_num_params", "nsg_mlp_init", "nsg_mlp_set_weights", "nsg_mlp_get_weights",
     "nsg_mlp_collect", "nsg_mlp_dataset", "nsg_mlp_train", "nsg_mlp_grad", "nsg_mlp_predict",
-    "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc",
+    "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc", "nsg_probe_latency",
 ]
 
 
@@ -110,6 +110,7 @@ def lib() -> C.CDLL:
         "nsg_tune_set": [P, P, C.c_int],
         "nsg_autotune": [P, C.c_int, C.c_char_p, C.c_int],
         "nsg_sort_device_noalloc": [P, P, P, P, P, I64, P],
+        "nsg_probe_latency": [P, C.c_int],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -362,6 +363,20 @@ def probe_fp64() -> dict:
         raise NsgError(rc, lib().nsg_last_error(None).decode())
     keys = ["dfma_tflops", "div_hw_gps", "div_int_gps", "fma_latency_cycles", "div_latency_cycles"]
     return {k: v.value for k, v in zip(keys, vals)}
+
+
+LATENCY_PROBES = ["fp64_fma", "fp64_fma_two_chains_one_warp", "fp64_fma_one_chain_two_warps",
+                  "div_fp64_pipe", "div_int_throughput_form", "div_latency_form", "imad32", "mulhi64",
+                  "i2f_fmul_f2i", "levi_civita_substep", "levi_civita_substep_zero_gravity"]
+
+
+def probe_latency() -> dict:
+    """Dependent latencies in cycles per iteration (see nsg_probe_latency)."""
+    v = np.zeros(len(LATENCY_PROBES))
+    rc = lib().nsg_probe_latency(_ptr(v), len(v))
+    if rc != NSG_OK:
+        raise NsgError(rc, lib().nsg_last_error(None).decode())
+    return dict(zip(LATENCY_PROBES, v.tolist()))
 
 
 def sort_particles(ctx: Context, particles: np.ndarray):

@@ -26,6 +26,8 @@
 // The force at the end of one substep is the force at the start of the next
 // (nsphere.c:2014 and :2022 evaluate forceLCfun at the same rho), so it is
 // evaluated once.
+#include <cstring>
+
 #include "nsg_internal.cuh"
 
 namespace nsg {
@@ -746,6 +748,65 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
             }
         }
     }
+}
+
+// Cycles per substep of lc_tau_step (fast form, PAIR) in a fallback tau-step that
+// one warp runs alone on an SM: split force (nonzero gravity numerator) and zero
+// gravity.  Synthetic inputs; the tolerance 1e-300 keeps every level from converging.
+template <bool ZG>
+__global__ void __launch_bounds__(32) k_lc_probe(StepArgs a, double gn, long long *cyc, double *out)
+{
+    __shared__ double xs[2304];
+    __shared__ int abandon;
+    const int lane = threadIdx.x & 31, role = lane & 15;
+    if (lane == 0) abandon = 0;
+    __syncwarp();
+    const int nlev = a.nlev;
+    int my_sub = 0;
+    if (role == 0) my_sub = 3;
+    else if (role <= nlev) my_sub = 4 * (1 << (role - 1)) + 1;
+    else if (role == nlev + 1) my_sub = 4 * (1 << nlev) + 1;
+    const int fb = 4 * (1 << nlev) + 1;
+    const double dtau = my_sub ? __ddiv_rn(1.0e-3, (double)my_sub) : 0.0, hdt = dmul(0.5, dtau);
+    const int64_t off = my_sub ? lc_slot(role, nlev) : 0;
+    bool bad = false;
+    const long long t0 = clock64();
+    LcTau o = lc_tau_step<true, true, ZG, int>(a, 0.0156, 0.03, 0.0, gn, 5.6e-11, dtau, hdt, my_sub, fb, nlev,
+                                               xs + off, &abandon, bad);
+    asm volatile("" : "+d"(o.r), "+d"(o.v));
+    const long long t1 = clock64();
+    out[lane] = o.r + o.v + o.lv + (bad ? 1.0 : 0.0);
+    if (lane == 0) cyc[0] = t1 - t0;
+}
+
+int lc_probe_substep(double *cycles_split, double *cycles_zero_gravity)
+{
+    StepArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nlev = 8;                                  // lc_slots(8) = 2056 <= 2304
+    a.tol_r = 1e-300;
+    a.tol_v = 1e-300;
+    a.out_type = 2;
+    long long *cyc = nullptr;
+    double *out = nullptr;
+    cudaError_t e = cudaMalloc((void **)&cyc, sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&out, 32 * sizeof(double));
+    for (int zg = 0; zg < 2 && e == cudaSuccess; zg++) {
+        for (int rep = 0; rep < 2 && e == cudaSuccess; rep++) {
+            if (zg) k_lc_probe<true><<<1, 32>>>(a, -0.0, cyc, out);
+            else k_lc_probe<false><<<1, 32>>>(a, -2.4e-7, cyc, out);
+            e = cudaDeviceSynchronize();
+        }
+        long long h = 0;
+        if (e == cudaSuccess) e = cudaMemcpy(&h, cyc, sizeof(h), cudaMemcpyDeviceToHost);
+        const double v = (double)h / (4 * (1 << a.nlev) + 1);
+        if (zg) *cycles_zero_gravity = v;
+        else *cycles_split = v;
+    }
+    cudaFree(cyc);
+    cudaFree(out);
+    if (e != cudaSuccess) return cuda_err(nullptr, e, "levi-civita substep probe");
+    return NSG_OK;
 }
 
 int lc_setup(nsg_ctx *c)

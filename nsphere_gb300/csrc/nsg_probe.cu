@@ -6,6 +6,9 @@
 // current device: FP64 FMA throughput (all SMs, independent chains), IEEE double
 // division throughput on the FP64 pipe and on the integer pipe (nsg_div.cuh), and
 // the dependent latency of one FP64 FMA and one division for a single warp.
+// nsg_probe_latency measures the dependent latencies the Levi-Civita chains are
+// built around (FP64, the three divisions, integer multiply, conversions) and the
+// cycles of one leading-warp substep of the Levi-Civita kernel.
 #include "nsg_internal.cuh"
 
 namespace nsg {
@@ -44,9 +47,74 @@ __global__ void k_probe_latency(double *out, long long *cyc, int iters, int kind
     if (threadIdx.x == 0) cyc[0] = t1 - t0;
 }
 
+// Dependent-latency probes, one block on one SM, cycles per iteration from the SM
+// clock.  The asm statements pin the chains between the two clock reads.
+// kind: 0 DFMA chain; 1 two independent DFMA chains in one warp; 2 one DFMA chain in
+// each of two warps; 3 dadd + __ddiv_rn; 4 dadd + div_rn; 5 dadd + div_rn_lat;
+// 6 IMAD; 7 mul.hi.u64; 8 I2F + FMUL + F2I.
+__global__ void k_probe_chain(double *out, long long *cyc, int iters, int kind)
+{
+    const int t = threadIdx.x;
+    double x = 1.5 + t * 1e-9, y = 2.5 + t * 1e-9;
+    uint64_t u = 0x9E3779B97F4A7C15ull + t;
+    uint32_t w = 12345u + t;
+    bool ok = true;
+    asm volatile("" : "+d"(x), "+d"(y), "+l"(u), "+r"(w));
+    const long long t0 = clock64();
+    asm volatile("" : "+d"(x), "+d"(y), "+l"(u), "+r"(w));
+    switch (kind) {
+    case 0: case 2:
+        for (int i = 0; i < iters; i++) x = fma(x, 1.0000001, 1e-12);
+        break;
+    case 1:
+        for (int i = 0; i < iters; i++) { x = fma(x, 1.0000001, 1e-12); y = fma(y, 0.9999999, 1e-12); }
+        break;
+    case 3: for (int i = 0; i < iters; i++) x = __ddiv_rn(0.7, __dadd_rn(x, 1.0)); break;
+    case 4: for (int i = 0; i < iters; i++) x = div_rn(0.7, __dadd_rn(x, 1.0)); break;
+    case 5: for (int i = 0; i < iters; i++) { bool o; x = div_rn_lat(0.7, __dadd_rn(x, 1.0), o); ok &= o; } break;
+    case 6: for (int i = 0; i < iters; i++) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(w) : "r"(2654435761u), "r"(7u)); break;
+    case 7: for (int i = 0; i < iters; i++) asm volatile("mul.hi.u64 %0, %0, %1;" : "+l"(u) : "l"(0xD1B54A32D192ED03ull)); break;
+    default: for (int i = 0; i < iters; i++) w = __float2uint_rz(__uint2float_rz(w) * 0.999f) + 7u; break;
+    }
+    asm volatile("" : "+d"(x), "+d"(y), "+l"(u), "+r"(w));
+    const long long t1 = clock64();
+    out[t] = x + y + (double)(u & 1023) + (double)w + (ok ? 0.0 : 1.0);
+    if (t == 0) cyc[0] = t1 - t0;
+}
+
 }  // namespace nsg
 
 using namespace nsg;
+
+extern "C" int nsg_probe_latency(double *cycles, int count)
+{
+    if (!cycles || count < 1) return set_err(nullptr, NSG_EINVAL, "latency probe needs an output array");
+    double *out = nullptr;
+    long long *cyc = nullptr;
+    cudaError_t e = cudaMalloc((void **)&out, 64 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&cyc, sizeof(long long));
+    const int n = count < 11 ? count : 11;
+    for (int k = 0; k < n && e == cudaSuccess; k++) {
+        long long h = 0;
+        const int it = 1024;
+        if (k <= 8) {
+            for (int rep = 0; rep < 2 && e == cudaSuccess; rep++) {
+                k_probe_chain<<<1, k == 2 ? 64 : 32>>>(out, cyc, it, k);
+                e = cudaDeviceSynchronize();
+            }
+            if (e == cudaSuccess) e = cudaMemcpy(&h, cyc, sizeof(h), cudaMemcpyDeviceToHost);
+            cycles[k] = (double)h / it;
+        } else {
+            double v[2] = {0.0, 0.0};
+            if (int rc = lc_probe_substep(&v[0], &v[1])) { cudaFree(out); cudaFree(cyc); return rc; }
+            cycles[k] = v[k - 9];
+        }
+    }
+    cudaFree(out);
+    cudaFree(cyc);
+    if (e != cudaSuccess) return cuda_err(nullptr, e, "latency probe");
+    return NSG_OK;
+}
 
 extern "C" int nsg_probe_fp64(double *dfma_tflops, double *div_hw_gps, double *div_int_gps,
                               double *fma_latency_cycles, double *div_latency_cycles)

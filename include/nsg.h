@@ -162,6 +162,24 @@ int nsg_sort_particles(nsg_ctx *ctx, double *const *particles, int64_t npts);
 int nsg_sort_device_noalloc(double *d_r, double *d_vr, double *d_ell, int32_t *d_id, double *d_aux,
                             int64_t npts, void *stream);
 
+/* The initial-conditions file of write_initial_conditions / read_initial_conditions
+ * (nsphere.c:2386-2487): int32 npts, then npts records of five doubles (r, v_r, ell,
+ * original index, mu).  nsg_write_init writes the resident state in its current
+ * order (mu = 0 unless carry_aux); nsg_read_init uploads a file's state like
+ * nsg_upload (expected_n < 0 accepts any count; otherwise a different count is an
+ * error, where the reference prints a warning and keeps its arrays). */
+int nsg_write_init(nsg_ctx *ctx, const char *filename);
+int nsg_read_init(nsg_ctx *ctx, const char *filename, int64_t expected_n);
+
+/* The all_particle_data stream (nsphere.c:1295-1324, 6452-6564).  Each nsg_snapshot
+ * appends, for every particle in original-id order, a 16-byte record {int32 rank
+ * in the last sort, float r, float v_r, float ell} of the resident state; records are
+ * packed on the GPU and written by a background thread while later steps run (two
+ * snapshots in flight; a third waits).  nsg_snapshot_close drains and closes. */
+int nsg_snapshot_open(nsg_ctx *ctx, const char *filename, int append);
+int nsg_snapshot(nsg_ctx *ctx);
+int nsg_snapshot_close(nsg_ctx *ctx);
+
 /* Looks up k particles by id -- the inverse_map reads of the tracking code
  * (nsphere.c:5845-5866, 6384-6450).  rank receives the current array index. */
 int nsg_gather(nsg_ctx *ctx, const int32_t *ids, int k, double *r, double *vr,

@@ -35,6 +35,7 @@ EXPORTS = [
     "nsg_mlp_num_params", "nsg_mlp_init", "nsg_mlp_set_weights", "nsg_mlp_get_weights",
     "nsg_mlp_collect", "nsg_mlp_dataset", "nsg_mlp_train", "nsg_mlp_grad", "nsg_mlp_predict",
     "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc", "nsg_probe_latency",
+    "nsg_write_init", "nsg_read_init", "nsg_snapshot_open", "nsg_snapshot", "nsg_snapshot_close",
 ]
 
 
@@ -111,6 +112,11 @@ def lib() -> C.CDLL:
         "nsg_autotune": [P, C.c_int, C.c_char_p, C.c_int],
         "nsg_sort_device_noalloc": [P, P, P, P, P, I64, P],
         "nsg_probe_latency": [P, C.c_int],
+        "nsg_write_init": [P, C.c_char_p],
+        "nsg_read_init": [P, C.c_char_p, I64],
+        "nsg_snapshot_open": [P, C.c_char_p, C.c_int],
+        "nsg_snapshot": [P],
+        "nsg_snapshot_close": [P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -317,6 +323,31 @@ class Context:
 
     def profile(self, enable: bool = True):
         self._check(self._L.nsg_profile(self._h, 1 if enable else 0))
+
+    def _n_from_ctx(self) -> int:
+        n = C.c_int64()
+        self._check(self._L.nsg_device_state(self._h, None, None, None, None, C.byref(n)))
+        return n.value
+
+    # ---- files of the reference
+    def write_init(self, path: str):
+        """Writes the reference's initial-conditions file from the resident state."""
+        self._check(self._L.nsg_write_init(self._h, os.fsencode(path)))
+
+    def read_init(self, path: str, expected_n: int = -1):
+        """Uploads the state of a reference initial-conditions file."""
+        self._check(self._L.nsg_read_init(self._h, os.fsencode(path), int(expected_n)))
+        self.n = self._n_from_ctx()
+
+    def snapshot_open(self, path: str, append: bool = False):
+        self._check(self._L.nsg_snapshot_open(self._h, os.fsencode(path), int(append)))
+
+    def snapshot(self):
+        """Appends an all_particle_data snapshot of the resident state (asynchronous)."""
+        self._check(self._L.nsg_snapshot(self._h))
+
+    def snapshot_close(self):
+        self._check(self._L.nsg_snapshot_close(self._h))
 
     def tune_get(self):
         """Launch shapes: (gather_level0 threads, its blocks/SM, log2 bucket, level blocks/SM)."""

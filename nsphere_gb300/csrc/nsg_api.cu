@@ -386,6 +386,7 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
 void nsg_destroy(nsg_ctx *c)
 {
     if (!c) return;
+    snap_close(c);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->side) cudaStreamSynchronize(c->side);
     for (auto ev : c->ev_pool) cudaEventDestroy(ev);
@@ -942,4 +943,22 @@ int nsg_profile_read(nsg_ctx *c, nsg_kernel_stat *stats, int max, int *count)
 int nsg::set_halos(nsg_ctx *c, const int64_t *seg_n, int nseg)
 {
     return setup_segments(c, seg_n, nseg);
+}
+
+int nsg::begin_upload(nsg_ctx *c, int64_t n)
+{
+    return upload_common(c, n);
+}
+
+int nsg::finish_upload_ids(nsg_ctx *c)
+{
+    cudaError_t e = cudaMemsetAsync(&c->ctr->pad, 0, 4, c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "id staging");
+    k_ids_from_double<<<grid_for(c, c->n, 256), 256, 0, c->stream>>>(c->stage_d, c->id[0], c->n, &c->ctr->pad);
+    return validate_ids(c, c->id[0], c->n, 0);
+}
+
+void nsg::build_inv(nsg_ctx *c)
+{
+    k_build_inv<<<grid_for(c, c->n, 256), 256, 0, c->stream>>>(c->id[c->cur], c->n, c->inv);
 }

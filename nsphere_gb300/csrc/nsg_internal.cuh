@@ -44,6 +44,7 @@ struct DevCounters {
 };
 
 struct MlpDev;   // nsg_mlp.cu
+struct SnapWriter;   // nsg_io.cu
 
 struct KernelStat {
     std::string name;
@@ -116,6 +117,9 @@ struct nsg_ctx {
 
     // staging for uploads of ids given as doubles
     double *stage_d = nullptr;
+
+    // snapshot stream (nsg_io.cu), open between nsg_snapshot_open and _close
+    nsg::SnapWriter *snap = nullptr;
 
     // learned level scheduler (nsg_mlp.cu)
     nsg::MlpDev *mlp = nullptr;
@@ -267,6 +271,10 @@ int bucket_sort_perm(nsg_ctx *c);                     // near-sorted fast path (
 inline Seg seg_table(const nsg_ctx *c) { return Seg{c->d_seg_start, c->d_bbase, c->nseg, c->tune.bshift}; }
 void drop_graph(nsg_ctx *c);                          // forget the captured step graph
 int set_halos(nsg_ctx *c, const int64_t *seg_n, int nseg);  // halo table + bucket layout
+int begin_upload(nsg_ctx *c, int64_t n);              // size the buffers for a one-halo state
+int finish_upload_ids(nsg_ctx *c);                    // ids staged as doubles -> int32, validated
+void build_inv(nsg_ctx *c);                           // inv from the current id order
+void snap_close(nsg_ctx *c);                          // end a snapshot stream (nsg_io.cu)
 int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred);  // predicted level per sorted position
 int mlp_features_sorted(nsg_ctx *c);                  // features of the sort (training set)
 int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)

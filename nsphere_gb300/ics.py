@@ -129,3 +129,54 @@ def hernquist(n: int, seed: int = 2, r_max: float = 100.0, r_a: float | None = N
     v = np.sqrt(wr * wr + vt * vt)
     mu2 = np.where(v > 0, wr / np.where(v > 0, v, 1.0), 0.0)
     return _finish(r, v, mu2)
+
+
+# ---------------------------------------------------------------- reference file formats
+
+INIT_RECORD = np.dtype([("r", "<f8"), ("v", "<f8"), ("l", "<f8"), ("id", "<f8"), ("mu", "<f8")])
+SNAP_RECORD = np.dtype([("rank", "<i4"), ("r", "<f4"), ("v", "<f4"), ("l", "<f4")])
+
+
+def write_init_file(path, r, vr, ell, ids, mu=None):
+    """Writes the initial-conditions file of the reference's write_initial_conditions
+    (nsphere.c:2386-2420): int32 npts, then npts records (r, v_r, ell, index, mu)."""
+    n = len(r)
+    rec = np.empty(n, dtype=INIT_RECORD)
+    rec["r"], rec["v"], rec["l"] = r, vr, ell
+    rec["id"] = np.asarray(ids, dtype=np.float64)
+    rec["mu"] = 0.0 if mu is None else mu
+    with open(path, "wb") as f:
+        f.write(np.int32(n).tobytes())
+        f.write(rec.tobytes())
+
+
+def read_init_file(path):
+    """Reads a file written by write_initial_conditions: (r, v_r, ell, ids, mu)."""
+    with open(path, "rb") as f:
+        n = int(np.frombuffer(f.read(4), dtype="<i4")[0])
+        rec = np.frombuffer(f.read(n * INIT_RECORD.itemsize), dtype=INIT_RECORD)
+    if rec.shape[0] != n:
+        raise ValueError("%s ends before its %d records" % (path, n))
+    return (rec["r"].copy(), rec["v"].copy(), rec["l"].copy(), rec["id"].astype(np.int32), rec["mu"].copy())
+
+
+def read_snapshots(path, n):
+    """Reads an all_particle_data stream (nsphere.c:1295-1324): array (snapshots, n)
+    of records (rank, r, v, l) indexed by original particle id."""
+    raw = np.fromfile(path, dtype=SNAP_RECORD)
+    if raw.size % n:
+        raise ValueError("%s does not hold whole snapshots of %d records" % (path, n))
+    return raw.reshape(-1, n)
+
+
+def snapshot_records(r, vr, ell, ids):
+    """The snapshot records the reference writes for a state in sorted order
+    (nsphere.c:6466-6476): record[id] = (rank, float r, float v_r, float ell)."""
+    n = len(r)
+    out = np.empty(n, dtype=SNAP_RECORD)
+    ids = np.asarray(ids, dtype=np.int64)
+    out["rank"][ids] = np.arange(n, dtype=np.int32)
+    out["r"][ids] = np.asarray(r).astype(np.float32)
+    out["v"][ids] = np.asarray(vr).astype(np.float32)
+    out["l"][ids] = np.asarray(ell).astype(np.float32)
+    return out

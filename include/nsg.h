@@ -56,6 +56,11 @@ extern "C" {
 #define NSG_ST_NOT_CONVERGED 0x4u /* a particle used its last level without converging */
 #define NSG_ST_SORT_FALLBACK 0x8u /* the near-sorted bucket sort overflowed; the full radix sort ran */
 #define NSG_ST_QUEUE 0x10u        /* a work queue overflowed (internal error) */
+#define NSG_ST_IC_REJECT 0x20u    /* an initial-condition rejection loop gave up (nsg_generate) */
+
+/* Initial-condition models of nsg_generate. */
+#define NSG_IC_PLUMMER 1    /* Plummer sphere, Aarseth-Henon-Wielen speeds */
+#define NSG_IC_HERNQUIST 2  /* Hernquist sphere truncated at r_max, isotropic f(E) */
 
 typedef struct nsg_params {
     double G;              /* effective gravitational constant: VEL_CONV_SQ*G_CONST (nsphere.c:365,373); 1 in G=M=1 units */
@@ -161,6 +166,13 @@ int nsg_sort_particles(nsg_ctx *ctx, double *const *particles, int64_t npts);
  * device share the scratch and race: keep them on one stream. */
 int nsg_sort_device_noalloc(double *d_r, double *d_vr, double *d_ell, int32_t *d_id, double *d_aux,
                             int64_t npts, void *stream);
+
+/* Generates n particles of a seeded model on the GPU into the resident state (G = M =
+ * a = 1, ids = radial rank, mu in the fifth column when carry_aux), in place of the
+ * reference's GSL-based generators (nsphere.c:4238-4824); r_max is the Hernquist
+ * truncation radius (ignored for Plummer).  Counter-based draws: the result depends
+ * only on (model, n, seed, r_max). */
+int nsg_generate(nsg_ctx *ctx, int model, int64_t n, uint64_t seed, double r_max);
 
 /* The initial-conditions file of write_initial_conditions / read_initial_conditions
  * (nsphere.c:2386-2487): int32 npts, then npts records of five doubles (r, v_r, ell,

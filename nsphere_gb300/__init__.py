@@ -21,6 +21,8 @@ NSG_EINVAL, NSG_ECUDA, NSG_ENOMEM, NSG_ESTATE, NSG_EIDS, NSG_EDEVICE, NSG_ETIMEO
 METHOD_KDK, METHOD_ADAPTIVE, METHOD_ADAPTIVE_LC = 2, 3, 5
 LC_RCRIT, LC_RADIUS, LC_OFF = 0, 1, 2
 SCHED_PLAIN, SCHED_LEARNED = 0, 1
+IC_PLUMMER, IC_HERNQUIST = 1, 2
+ST_IC_REJECT = 0x20
 ST_NAN, ST_TAU_CAP, ST_NOT_CONVERGED, ST_SORT_FALLBACK, ST_QUEUE = 0x1, 0x2, 0x4, 0x8, 0x10
 
 # exported symbols of include/nsg.h (tests check the library exports each one)
@@ -36,6 +38,7 @@ EXPORTS = [
     "nsg_mlp_collect", "nsg_mlp_dataset", "nsg_mlp_train", "nsg_mlp_grad", "nsg_mlp_predict",
     "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc", "nsg_probe_latency",
     "nsg_write_init", "nsg_read_init", "nsg_snapshot_open", "nsg_snapshot", "nsg_snapshot_close",
+    "nsg_generate",
 ]
 
 
@@ -113,6 +116,7 @@ def lib() -> C.CDLL:
         "nsg_sort_device_noalloc": [P, P, P, P, P, I64, P],
         "nsg_probe_latency": [P, C.c_int],
         "nsg_write_init": [P, C.c_char_p],
+        "nsg_generate": [P, C.c_int, I64, C.c_uint64, D],
         "nsg_read_init": [P, C.c_char_p, I64],
         "nsg_snapshot_open": [P, C.c_char_p, C.c_int],
         "nsg_snapshot": [P],
@@ -328,6 +332,11 @@ class Context:
         n = C.c_int64()
         self._check(self._L.nsg_device_state(self._h, None, None, None, None, C.byref(n)))
         return n.value
+
+    def generate(self, model: int, n: int, seed: int, r_max: float = 100.0):
+        """Seeded initial conditions generated on the GPU into the resident state."""
+        self._check(self._L.nsg_generate(self._h, int(model), int(n), int(seed), float(r_max)))
+        self.n = int(n)
 
     # ---- files of the reference
     def write_init(self, path: str):

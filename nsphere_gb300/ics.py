@@ -180,3 +180,116 @@ def snapshot_records(r, vr, ell, ids):
     out["v"][ids] = np.asarray(vr).astype(np.float32)
     out["l"][ids] = np.asarray(ell).astype(np.float32)
     return out
+
+
+# ---------------------------------------------------------------- counter-based generators
+# The restatement, in numpy, of the GPU generators of nsg_generate (csrc/nsg_ics.cu):
+# the same counter-based draws and the same arithmetic, for the tests.
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _mix(x):
+    x = x + np.uint64(0x9E3779B97F4A7C15)
+    x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return x ^ (x >> np.uint64(31))
+
+
+def counter_uniform(seed, i, j):
+    """Draw j of particle i in [0, 1): SplitMix64 finaliser applied twice."""
+    with np.errstate(over="ignore"):
+        i = np.asarray(i, dtype=np.uint64)
+        h = _mix(_mix(np.uint64(seed) ^ (i * np.uint64(0xD1B54A32D192ED03))) + np.uint64(j))
+    return (h >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+
+
+def _hq_df_unnormalised(eps):
+    e = np.clip(eps, 0.0, 1.0 - 1e-15)
+    q = np.sqrt(e)
+    q2 = q * q
+    val = 3.0 * np.arcsin(q) + q * np.sqrt(1.0 - q2) * (1.0 - 2.0 * q2) * (8.0 * q2 * q2 - 8.0 * q2 - 3.0)
+    w = 1.0 - q2
+    return val / (w * w * np.sqrt(w))
+
+
+def _hq_target(psi, x):
+    return x * x * _hq_df_unnormalised(psi * (1.0 - x * x))
+
+
+def _hq_bound(psi):
+    """Per-particle rejection bound: best of x_j = (j/64)^2, 40 golden-section steps."""
+    gb = np.full(psi.shape, -1.0)
+    jb = np.ones(psi.shape, dtype=np.int64)
+    for j in range(1, 65):
+        t = j / 64.0
+        g = _hq_target(psi, t * t)
+        better = g > gb
+        gb = np.where(better, g, gb)
+        jb = np.where(better, j, jb)
+    tl = (jb - 1) / 64.0
+    th = np.where(jb < 64, jb + 1, 64) / 64.0
+    a, b = tl * tl, th * th
+    ig = 0.6180339887498949
+    c = b - ig * (b - a)
+    d = a + ig * (b - a)
+    gc, gd = _hq_target(psi, c), _hq_target(psi, d)
+    for _ in range(40):
+        left = gc > gd
+        nb = np.where(left, d, b)
+        na = np.where(left, a, c)
+        nc = np.where(left, nb - ig * (nb - na), d)
+        nd = np.where(left, c, na + ig * (nb - na))
+        ngc = np.where(left, _hq_target(psi, nc), gd)
+        ngd = np.where(left, gc, _hq_target(psi, nd))
+        a, b, c, d, gc, gd = na, nb, nc, nd, ngc, ngd
+    return np.maximum(gb, np.maximum(gc, gd)) * 1.3 + 1e-300
+
+
+def _rank_order(r, vr, ell, mu):
+    order = np.lexsort((np.arange(r.shape[0]), r))
+    return r[order], vr[order], ell[order], np.arange(r.shape[0], dtype=np.int32), mu[order]
+
+
+def plummer_counter(n: int, seed: int):
+    """(r, vr, ell, ids, mu) of nsg_generate(NSG_IC_PLUMMER, n, seed)."""
+    i = np.arange(n, dtype=np.uint64)
+    u = 1e-10 + (1.0 - 1e-10) * counter_uniform(seed, i, 0)
+    r = 1.0 / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
+    q = np.zeros(n)
+    todo = np.arange(n)
+    a = 0
+    while todo.size:
+        x1 = counter_uniform(seed, i[todo], 2 + 2 * a)
+        x2 = counter_uniform(seed, i[todo], 3 + 2 * a)
+        w = 1.0 - x1 * x1
+        ok = 0.1 * x2 < x1 * x1 * (w * w * w * np.sqrt(w))
+        q[todo[ok]] = x1[ok]
+        todo = todo[~ok]
+        a += 1
+    v = q * np.sqrt(2.0) / np.sqrt(np.sqrt(1.0 + r * r))
+    mu = 2.0 * counter_uniform(seed, i, 1) - 1.0
+    return _rank_order(r, v * mu, r * v * np.sqrt(np.maximum(0.0, 1.0 - mu * mu)), mu)
+
+
+def hernquist_counter(n: int, seed: int, r_max: float = 100.0):
+    """(r, vr, ell, ids, mu) of nsg_generate(NSG_IC_HERNQUIST, n, seed, r_max)."""
+    i = np.arange(n, dtype=np.uint64)
+    umax = (r_max / (1.0 + r_max)) * (r_max / (1.0 + r_max))
+    s = np.sqrt(umax * counter_uniform(seed, i, 0))
+    r = np.maximum(s / (1.0 - s), 1e-12)
+    psi = 1.0 / (1.0 + r)
+    bound = _hq_bound(psi)
+    x = np.zeros(n)
+    todo = np.arange(n)
+    a = 0
+    while todo.size:
+        xx = counter_uniform(seed, i[todo], 2 + 2 * a)
+        yy = counter_uniform(seed, i[todo], 3 + 2 * a) * bound[todo]
+        ok = yy < _hq_target(psi[todo], xx)
+        x[todo[ok]] = xx[ok]
+        todo = todo[~ok]
+        a += 1
+    w = x * np.sqrt(2.0 * psi)
+    mu = 2.0 * counter_uniform(seed, i, 1) - 1.0
+    return _rank_order(r, w * mu, r * w * np.sqrt(np.maximum(0.0, 1.0 - mu * mu)), mu)

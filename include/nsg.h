@@ -174,6 +174,14 @@ int nsg_sort_device_noalloc(double *d_r, double *d_vr, double *d_ell, int32_t *d
  * only on (model, n, seed, r_max). */
 int nsg_generate(nsg_ctx *ctx, int model, int64_t n, uint64_t seed, double r_max);
 
+/* Per-particle potential and energy of the post-processing (nsphere.c:7697-7846), on
+ * the resident state in its sorted order (sorted first if needed; one halo):
+ * psi[i] = G (M_i / r_i + dM sum_{j>i} 1/r_j) with M_i = (i+1) dM, dM = M_total / N;
+ * E[i] = psi[i] - ell_i^2/(2 r_i^2) - v_i^2/2; *psi0 = G dM sum_j 1/r_j.  psi, E are
+ * host arrays of n doubles (either may be NULL); the suffix sums are a parallel scan,
+ * so values agree with the reference's sequential sums to rounding. */
+int nsg_potential(nsg_ctx *ctx, double *psi, double *E, double *psi0);
+
 /* The initial-conditions file of write_initial_conditions / read_initial_conditions
  * (nsphere.c:2386-2487): int32 npts, then npts records of five doubles (r, v_r, ell,
  * original index, mu).  nsg_write_init writes the resident state in its current

@@ -38,7 +38,7 @@ EXPORTS = [
     "nsg_mlp_collect", "nsg_mlp_dataset", "nsg_mlp_train", "nsg_mlp_grad", "nsg_mlp_predict",
     "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc", "nsg_probe_latency",
     "nsg_write_init", "nsg_read_init", "nsg_snapshot_open", "nsg_snapshot", "nsg_snapshot_close",
-    "nsg_generate",
+    "nsg_generate", "nsg_potential",
 ]
 
 
@@ -117,6 +117,7 @@ def lib() -> C.CDLL:
         "nsg_probe_latency": [P, C.c_int],
         "nsg_write_init": [P, C.c_char_p],
         "nsg_generate": [P, C.c_int, I64, C.c_uint64, D],
+        "nsg_potential": [P, P, P, C.POINTER(D)],
         "nsg_read_init": [P, C.c_char_p, I64],
         "nsg_snapshot_open": [P, C.c_char_p, C.c_int],
         "nsg_snapshot": [P],
@@ -337,6 +338,14 @@ class Context:
         """Seeded initial conditions generated on the GPU into the resident state."""
         self._check(self._L.nsg_generate(self._h, int(model), int(n), int(seed), float(r_max)))
         self.n = int(n)
+
+    def potential(self):
+        """(psi, E, psi0) of the sorted resident state (see nsg_potential)."""
+        psi = np.empty(self.n)
+        E = np.empty(self.n)
+        p0 = C.c_double()
+        self._check(self._L.nsg_potential(self._h, _ptr(psi), _ptr(E), C.byref(p0)))
+        return psi, E, p0.value
 
     # ---- files of the reference
     def write_init(self, path: str):

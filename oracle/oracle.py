@@ -175,3 +175,25 @@ class Reference:
 
     def num_threads(self):
         return self.L.ref_num_threads()
+
+
+def potential_energy(r, vr, ell, G=1.0, M=1.0):
+    """The reference's post-processing potential and energies (nsphere.c:7697-7846) on a
+    state in sorted order, in its sequential summation order: (psi, E, psi0)."""
+    import numpy as np
+    n = len(r)
+    dM = M / n
+    inv = 1.0 / r
+    suffix = np.empty(n)
+    acc = 0.0
+    for j in range(n - 1, -1, -1):
+        acc = acc + inv[j]
+        suffix[j] = acc
+    after = np.concatenate([suffix[1:], [0.0]])
+    Mr = (np.arange(n) + 1.0) * dM
+    psi = G * ((Mr / r) + dM * after)
+    E = psi - (ell * ell / (2.0 * r * r)) - 0.5 * vr * vr
+    s = 0.0
+    for j in range(n):
+        s += inv[j]
+    return psi, E, G * dM * s

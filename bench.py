@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--n", type=int, default=10_000_000)
     ap.add_argument("--workload", choices=["adaptive", "kdk"], default="adaptive")
     ap.add_argument("--sched", choices=["plain", "learned"], default="plain")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--ab-steps", type=int, default=8, help="steps of the learned/plain comparison (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -884,10 +884,6 @@ int integrate_adaptive(nsg_ctx *c)
     if (int rc = sort_perm(c)) return rc;
     StepArgs a = make_args(c);
     const bool learned = (c->p.sched == NSG_SCHED_LEARNED) && a.nlev > 1;
-    if (learned)
-        if (int rc = mlp_predict_sorted(c, &a.pred)) return rc;
-    if (c->mlp_collect)
-        if (int rc = mlp_features_sorted(c)) return rc;
     cudaStream_t s = c->stream;
     cudaError_t e;
     // reset queue counters (qcount[] and lc_count live at the head of DevCounters)
@@ -920,6 +916,11 @@ int integrate_adaptive(nsg_ctx *c)
             k_levi_civita_lanes<<<c->num_sms / 3, 32, c->lc_smem, s>>>(a);
         c->launches += 1;
     }
+    // the scheduler's features and predictions run beside the Levi-Civita chains too
+    if (learned)
+        if (int rc = mlp_predict_sorted(c, &a.pred, ls)) return rc;
+    if (c->mlp_collect)
+        if (int rc = mlp_features_sorted(c, ls)) return rc;
     {
         // algorithmic bytes: perm 4, gather r v ell id 28, write r v ell id 28, inv 4, level 1
         ProfScope ps(c, "gather_level0", (double)c->n * (4 + 28 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)), ls);

@@ -275,8 +275,8 @@ int begin_upload(nsg_ctx *c, int64_t n);              // size the buffers for a 
 int finish_upload_ids(nsg_ctx *c);                    // ids staged as doubles -> int32, validated
 void build_inv(nsg_ctx *c);                           // inv from the current id order
 void snap_close(nsg_ctx *c);                          // end a snapshot stream (nsg_io.cu)
-int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred);  // predicted level per sorted position
-int mlp_features_sorted(nsg_ctx *c);                  // features of the sort (training set)
+int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred, cudaStream_t st);  // predicted level per sorted position
+int mlp_features_sorted(nsg_ctx *c, cudaStream_t st);  // features of the sort (training set)
 int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)
 void mlp_free(nsg_ctx *c);
 int bucket_setup(nsg_ctx *c);

@@ -652,12 +652,12 @@ static MlpStepArgs step_args(nsg_ctx *c)
 }
 
 // Predicted class per sorted position of the sort just made (c->perm, copy c->cur).
-int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred)
+int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred, cudaStream_t st)
 {
     if (!c->mlp || !c->mlp->ready) return set_err(c, NSG_ESTATE, "learned schedule needs nsg_mlp_init or trained weights");
     if (int rc = mlp_ensure_n(c)) return rc;
-    ProfScope ps(c, "mlp_predict", (double)c->n * (4 + 28 + 1));
-    k_mlp_features<true><<<grid_for(c, c->n, 256, 4), 256, 0, c->stream>>>(step_args(c), *c->mlp);
+    ProfScope ps(c, "mlp_predict", (double)c->n * (4 + 28 + 1), st);
+    k_mlp_features<true><<<grid_for(c, c->n, 256, 4), 256, 0, st>>>(step_args(c), *c->mlp);
     c->launches += 1;
     *pred = c->mlp->pred;
     cudaError_t e = cudaGetLastError();
@@ -665,10 +665,10 @@ int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred)
 }
 
 // Features of the sort just made, kept for the training set (collect mode).
-int mlp_features_sorted(nsg_ctx *c)
+int mlp_features_sorted(nsg_ctx *c, cudaStream_t st)
 {
     if (int rc = mlp_ensure_n(c)) return rc;
-    k_mlp_features<false><<<grid_for(c, c->n, 256, 4), 256, 0, c->stream>>>(step_args(c), *c->mlp);
+    k_mlp_features<false><<<grid_for(c, c->n, 256, 4), 256, 0, st>>>(step_args(c), *c->mlp);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "mlp features");
 }

@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=10_000_000)
-    ap.add_argument("--workload", choices=["adaptive", "kdk"], default="adaptive")
+    ap.add_argument("--workload", choices=["adaptive", "kdk", "ensemble"], default="adaptive")
     ap.add_argument("--sched", choices=["plain", "learned"], default="plain")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--ab-steps", type=int, default=8, help="steps of the learned/plain comparison (0: skip)")
@@ -67,6 +67,14 @@ def workload(args, seed_offset=0):
                    dt=1e-3, method="fixed-step leapfrog (reference method 2)")
         state = ics.plummer(args.n, seed=1 + seed_offset)
         params = dict(dt=1e-3, method=2)
+    elif args.workload == "ensemble":
+        r, vr, ell, ids, sizes = ics.plummer_ensemble(256, 10_000, 1_000_000, seed=3 + seed_offset)
+        cfg = dict(workload="plummer_ensemble_adaptive_lc", n=int(len(r)), halos=256,
+                   halo_n="log-uniform in [1e4, 1e6]", profile="plummer", seed=3 + seed_offset, dt=1e-3,
+                   max_levels=8, max_subdiv=128, lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
+        state = (r, vr, ell, ids, sizes)
+        params = dict(dt=1e-3, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
+        args.n = int(len(r))
     else:
         cfg = dict(workload="hernquist_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 isotropic",
                    seed=2 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,
@@ -226,7 +234,8 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     # independent replica per rank (the path does not shard across GPUs)
     cfg, state, params = workload(args, seed_offset=rank)
-    r, vr, ell, ids = state
+    r, vr, ell, ids = state[:4]
+    sizes = state[4] if len(state) > 4 else None
     n = len(r)
     fp64 = ns.probe_fp64()
     fp64["latency_cycles"] = ns.probe_latency()
@@ -238,7 +247,12 @@ def main():
     if args.sched == "learned":
         p.sched = ns.SCHED_LEARNED
     ctx = ns.Context(p, stream=stream.cuda_stream)
-    ctx.upload(r, vr, ell, ids)
+    if sizes is None:
+        ctx.upload(r, vr, ell, ids)
+    else:
+        ctx.upload_ensemble(r, vr, ell, ids, sizes)
+        ctx.step(1)
+        cfg["tuned_shapes"] = ctx.autotune(steps=1)["chosen"]
     E0 = sum(ctx.energy())
     ctx.step(args.warmup)
     torch.cuda.synchronize()
@@ -331,8 +345,12 @@ def main():
     barrier()
     ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ee0.record(stream)
+    hn = None if sizes is None else np.ascontiguousarray(sizes, dtype=np.int64)
     for _ in range(args.e2e_steps):
-        ctx._check(lib.nsg_upload(ctx.handle, P(h_r), P(h_v), P(h_l), P(h_i), None, n))
+        if hn is None:
+            ctx._check(lib.nsg_upload(ctx.handle, P(h_r), P(h_v), P(h_l), P(h_i), None, n))
+        else:
+            ctx._check(lib.nsg_upload_ensemble(ctx.handle, P(h_r), P(h_v), P(h_l), P(h_i), None, P(hn), len(hn)))
         ctx._check(lib.nsg_step(ctx.handle, 1))
         ctx._check(lib.nsg_download(ctx.handle, P(o_r), P(o_v), P(o_l), P(o_i), None))
     ee1.record(stream)
@@ -401,7 +419,7 @@ def main():
             "status": status,
             "learned_vs_plain": learned,
         }
-        if not args.no_cpu_baseline and world == 1:
+        if not args.no_cpu_baseline and world == 1 and sizes is None:
             line["cpu_baseline"] = cpu_baseline(state, params, args.cpu_seconds)
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -273,6 +273,89 @@ k_bucket_sort(const unsigned int *__restrict__ cnt, const unsigned int *__restri
     kmax = block_reduce_u64(kmax, false, red);
     const uint64_t diff = kmin ^ kmax;
     const int kbits = diff ? 64 - __clzll((long long)diff) : 0;
+    if (kbits > 16) {
+        // Fast form: two passes on a 16-bit quantised key q = (key - kmin) >> qs (monotone
+        // in the key), then each run of equal q -- a few elements at most for keys spread
+        // over 2^40 values -- is ordered by (key, id) by counting ranks.  A run longer than
+        // 32 sends the block to the full form below (any start order is fine for it).
+        // padding items (key ~0, positions >= m) clamp to the top value and, the passes
+        // being stable, stay behind every real item
+        const int qb = 64 - __clzll((long long)(kmax - kmin));
+        const int qs = qb > 16 ? qb - 16 : 0;
+        const uint64_t k0 = kmin;
+        for (int shift = 0; shift < 16; shift += 8)
+            block_radix_pass(k, v, J, [shift, qs, k0](uint64_t kk, uint64_t) {
+                const uint64_t q = (kk - k0) >> qs;
+                return (unsigned)((q < 0xffffull ? q : 0xffffull) >> shift) & 255u; }, whist, dtot, xk);
+        uint32_t fin[kBucketItems];
+        int too_long = 0;
+#pragma unroll
+        for (int j = 0; j < kBucketItems; j++)
+            if (j < J) xk[w * S + j * 32 + lane] = k[j];
+        __syncthreads();
+        uint32_t rs[kBucketItems], eqm[kBucketItems];   // run start | length << 16, equal-key mask
+#pragma unroll
+        for (int j = 0; j < kBucketItems; j++) {
+            const uint32_t pos = w * S + j * 32 + lane;
+            fin[j] = pos;
+            rs[j] = pos;
+            eqm[j] = 0;
+            if (j < J && pos < m) {
+                const uint64_t q = (k[j] - k0) >> qs;
+                uint32_t lo = pos, hi = pos + 1;
+                while (lo > 0 && pos - lo < 33 && ((xk[lo - 1] - k0) >> qs) == q) lo--;
+                while (hi < m && hi - pos < 33 && ((xk[hi] - k0) >> qs) == q) hi++;
+                const uint32_t len = hi - lo;
+                if (len > 32) too_long = 1;
+                else if (len > 1) {
+                    uint32_t less = 0, eq = 0;
+                    for (uint32_t t = 0; t < len; t++) {
+                        const uint64_t kq = xk[lo + t];
+                        less += kq < k[j];
+                        if (kq == k[j] && lo + t != pos) eq |= 1u << t;
+                    }
+                    fin[j] = lo + less;
+                    rs[j] = lo | (len << 16);
+                    eqm[j] = eq;
+                }
+            }
+        }
+        too_long = __syncthreads_or(too_long);
+        if (!too_long) {
+            // equal keys inside a run: by id (ids are distinct)
+#pragma unroll
+            for (int j = 0; j < kBucketItems; j++)
+                if (j < J) xk[w * S + j * 32 + lane] = v[j];
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < kBucketItems; j++) {
+                if (j < J && eqm[j]) {
+                    const uint32_t lo = rs[j] & 0xffffu, id = (uint32_t)(v[j] >> 32);
+                    uint32_t e = eqm[j], add = 0;
+                    while (e) {
+                        const int t = __ffs(e) - 1;
+                        e &= e - 1;
+                        add += (uint32_t)(xk[lo + t] >> 32) < id;
+                    }
+                    fin[j] += add;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < kBucketItems; j++) {
+                const uint32_t pos = w * S + j * 32 + lane;
+                if (j < J && pos < m) xk[fin[j]] = v[j];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < kBucketItems; j++) {
+                const uint32_t pos = w * S + j * 32 + lane;
+                if (j < J && pos < m) perm[base + pos] = (uint32_t)(xk[pos] & 0xffffffffu);
+            }
+            return;
+        }
+        __syncthreads();
+    }
     for (int shift = 0; shift < kbits; shift += 8)
         block_radix_pass(k, v, J, [shift](uint64_t kk, uint64_t) { return (unsigned)(kk >> shift) & 255u; },
                          whist, dtot, xk);

@@ -22,8 +22,8 @@
 
 namespace nsg {
 
-constexpr int kBucketThreads = 512;
-constexpr int kBucketItems = 12;
+constexpr int kBucketThreads = 1024;
+constexpr int kBucketItems = 6;
 constexpr int kBucketWarps = kBucketThreads / 32;
 
 
@@ -139,7 +139,7 @@ k_bucket_scan(const unsigned int *__restrict__ cnt, int nb, int cap, unsigned in
 // One stable LSD pass on 8 bits chosen by `digit_of`, over the block's items held
 // in registers.  Warp w owns positions [w*S, (w+1)*S) with S = J*32: item j < J of
 // lane l is position w*S + j*32 + l, so walking j and then lanes visits positions
-// in order and the match.any ranks are stable.  J = ceil(count / 512) adapts the
+// in order and the match.any ranks are stable.  J = ceil(count / 1024) adapts the
 // work to the bucket's fill; items are exchanged through shared memory.
 template <typename DigitFn>
 __device__ __forceinline__ void block_radix_pass(uint64_t (&k)[kBucketItems], uint64_t (&v)[kBucketItems],

@@ -21,7 +21,7 @@ constexpr int kRadixThreads = 256;
 constexpr int kRadixItems = 16;       // keys per thread per tile
 constexpr int kRadixTile = kRadixThreads * kRadixItems;
 constexpr int kReduceBlocks = 1024;   // fixed block count of energy partial sums
-constexpr int kBucketCap = 6144;      // entries one bucket block sorts (512 threads x 12)
+constexpr int kBucketCap = 6144;      // entries one bucket block sorts (1024 threads x 6)
 
 // Launch shapes chosen by the autotuner (nsg_tune.cu); defaults measured on GB300.
 struct Tune {

@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=10_000_000)
-    ap.add_argument("--workload", choices=["adaptive", "kdk", "ensemble"], default="adaptive")
+    ap.add_argument("--workload", choices=["adaptive", "kdk", "ensemble", "om", "stress"], default="adaptive")
     ap.add_argument("--sched", choices=["plain", "learned"], default="plain")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--ab-steps", type=int, default=8, help="steps of the learned/plain comparison (0: skip)")
@@ -75,6 +75,31 @@ def workload(args, seed_offset=0):
         state = (r, vr, ell, ids, sizes)
         params = dict(dt=1e-3, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
         args.n = int(len(r))
+    elif args.workload == "om":
+        cfg = dict(workload="hernquist_om_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 osipkov-merritt r_a=1",
+                   seed=4 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,
+                   lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
+        state = ics.hernquist(args.n, seed=4 + seed_offset, r_a=1.0)
+        params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
+    elif args.workload == "stress":
+        # Hernquist, 20 % of the particles on near-radial orbits (ell uniform in [0, 1e-4]),
+        # a central point mass ramped from 0 to 0.01 over 500 steps
+        # generated on the GPU (nsg_generate): the host generator is slow at 1e8
+        import nsphere_gb300 as ns
+        with ns.Context(ns.default_params()) as g:
+            g.generate(ns.IC_HERNQUIST, args.n, 5 + seed_offset, 100.0)
+            r, vr, ell, ids = g.download()
+        rng = np.random.default_rng(5 + seed_offset)
+        pick = rng.random(args.n) < 0.2
+        ell = ell.copy()
+        ell[pick] = rng.uniform(0.0, 1e-4, int(pick.sum()))
+        cfg = dict(workload="hernquist_radial_point_mass", n=args.n, profile="hernquist a=1 r<=100 isotropic",
+                   radial_fraction=0.2, radial_ell="U[0, 1e-4]", point_mass="0 -> 0.01 over 500 steps",
+                   seed=5 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,
+                   lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
+        state = (r, vr, ell, ids)
+        params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000,
+                      point_mass_rate=0.01 / (500 * 5e-4))
     else:
         cfg = dict(workload="hernquist_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 isotropic",
                    seed=2 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,
@@ -303,7 +328,7 @@ def main():
     # train on the GPU, then time the same steps under each schedule from one snapshot.
     # Both schedules give bit-identical states, so |dE/E| is equal by construction.
     learned = None
-    if args.workload == "adaptive" and args.ab_steps > 0:
+    if args.workload in ("adaptive", "om") and args.ab_steps > 0:
         ctx.mlp_init(4)
         ctx.mlp_collect(3, keep_level0=0.02, capacity=1 << 21)
         loss = ctx.mlp_train(epochs=4, batch=2048, lr=3e-3, seed=4)

@@ -43,6 +43,15 @@ double orc_gnum(int64_t i, int64_t n, double G, double M)
     return (-(G) * ((double)i / (double)n)) * M;
 }
 
+/* The gravity numerator with a central point mass Mpt, the build's extension for the
+ * point-mass configuration (the reference has none): gnum - G Mpt when Mpt != 0. */
+double orc_gnum_pm(int64_t i, int64_t n, double G, double M, double Mpt)
+{
+    double g = orc_gnum(i, n, G, M);
+    if (Mpt != 0.0) g = g - G * Mpt;
+    return g;
+}
+
 /* dv/dt = gravity + centrifugal, nsphere.c:502-515 and :532-535.
  * gravity = gnum / (r*r), centrifugal = (ell*ell) / (r*r*r). */
 static inline double acc_leap(double r, double gnum, double l2)
@@ -313,7 +322,7 @@ int64_t orc_step_adaptive(const orc_params *p, int64_t n, double *r, double *vr,
 #pragma omp parallel for schedule(dynamic, 64) reduction(+:capped)
     for (int64_t i = 0; i < n; i++) {
         double ri = r[i], vi = vr[i], li = ell[i];
-        double gnum = orc_gnum(i, n, p->G, p->M);
+        double gnum = orc_gnum_pm(i, n, p->G, p->M, p->point_mass);
         double rn, vn;
         int lv;
         if (use_lc(p, i, n, ri, li)) {
@@ -342,7 +351,7 @@ void orc_step_kdk(const orc_params *p, int64_t n, double *r, double *vr, double 
     double dt = p->dt;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; i++) {
-        double a = acc_leap(r[i], orc_gnum(i, n, p->G, p->M), ell[i] * ell[i]);
+        double a = acc_leap(r[i], orc_gnum_pm(i, n, p->G, p->M, p->point_mass), ell[i] * ell[i]);
         vr[i] = vr[i] + 0.5 * a * dt;
     }
 #pragma omp parallel for schedule(static)
@@ -350,7 +359,7 @@ void orc_step_kdk(const orc_params *p, int64_t n, double *r, double *vr, double 
     orc_sort(n, r, vr, ell, id, NULL);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; i++) {
-        double a = acc_leap(r[i], orc_gnum(i, n, p->G, p->M), ell[i] * ell[i]);
+        double a = acc_leap(r[i], orc_gnum_pm(i, n, p->G, p->M, p->point_mass), ell[i] * ell[i]);
         vr[i] = vr[i] + 0.5 * a * dt;
     }
 }
@@ -367,7 +376,7 @@ void orc_energy(const orc_params *p, int64_t n, const double *r, const double *v
     for (int64_t i = 0; i < n; i++) {
         double ri = r[i];
         k += 0.5 * m * (vr[i] * vr[i] + (ell[i] * ell[i]) / (ri * ri));
-        w += m * orc_gnum(i, n, p->G, p->M) / ri;
+        w += m * orc_gnum_pm(i, n, p->G, p->M, p->point_mass) / ri;
     }
     *K = k;
     *W = w;
@@ -387,6 +396,7 @@ void orc_params_default(orc_params *p)
     p->lc_alpha = 0.05;
     p->lc_radius = 1.0e-3;
     p->max_tau_steps = 100000000;
+    p->point_mass = 0.0;
 }
 
 int orc_num_threads(void)

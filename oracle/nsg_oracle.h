@@ -15,10 +15,12 @@ typedef struct orc_params {
     double lc_alpha;       /* 0.05 */
     double lc_radius;      /* 1e-3 */
     int64_t max_tau_steps; /* tau-step cap (reference 1e8) */
+    double point_mass;     /* central point mass added to M_i (not in the reference; 0 = reference) */
 } orc_params;
 
 void orc_params_default(orc_params *p);
 double orc_gnum(int64_t i, int64_t n, double G, double M);
+double orc_gnum_pm(int64_t i, int64_t n, double G, double M, double Mpt);
 void orc_micro_leap(double r_in, double v_in, double l2, double gnum, double h,
                     int64_t N, int fine, double *r_out, double *v_out);
 void orc_adaptive_leap(double r_in, double v_in, double ell, double gnum, double h,

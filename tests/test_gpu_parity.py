@@ -190,6 +190,30 @@ def test_multi_step_adaptive(nsg, oracle):
     assert np.array_equal(gid, cur[3]) and np.array_equal(gr, cur[0]) and np.array_equal(gv, cur[1])
 
 
+@pytest.mark.parametrize("method", [2, 5])
+def test_point_mass_ramp_matches_oracle(nsg, oracle, method):
+    """Central point mass (the stress configuration; not in the reference): every step
+    uses the current mass in the gravity numerator, then the mass grows by rate*dt."""
+    n, dt, m0, rate = 12000, 1e-3, 1e-3, 0.5
+    # in radial order, as the reference sorts once before its time loop (nsphere.c:5339-5342)
+    r, vr, ell, ids = oracle.sort(*_adaptive_case(n, 44, lowl=200))
+    kw = dict(dt=dt, max_subdiv=64, lc_rule=1, lc_radius=2e-2) if method == 5 else dict(dt=dt)
+    p = oracle.params(point_mass=m0, **kw)
+    cur = (r, vr, ell, ids)
+    for _ in range(6):
+        cur = (oracle.step_adaptive(p, *cur) if method == 5 else oracle.step_kdk(p, *cur))[:4]
+        p.point_mass = p.point_mass + rate * dt
+    srt = oracle.sort(*cur)                  # energies are taken over the current radial order
+    K, W = oracle.energy(p, srt[0], srt[1], srt[2])
+    with _ctx(nsg, method=method, point_mass=m0, point_mass_rate=rate, **kw) as c:
+        c.upload(r, vr, ell, ids)
+        c.step(6)
+        gr, gv, gl, gid = c.download()
+        gK, gW = c.energy()
+    assert np.array_equal(gid, cur[3]) and np.array_equal(gr, cur[0]) and np.array_equal(gv, cur[1])
+    assert gK == pytest.approx(K, rel=1e-12) and gW == pytest.approx(W, rel=1e-12)
+
+
 def test_energy_and_gather(nsg, oracle):
     n = 50000
     r, vr, ell, ids = ics.plummer(n, seed=5)

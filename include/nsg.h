@@ -82,6 +82,11 @@ typedef struct nsg_params {
     int32_t graph;         /* 1: repeat steps by replaying a captured CUDA graph of two steps (default) */
     double point_mass;     /* central point mass added to M_i at the step start (0 = reference) */
     double point_mass_rate;/* d(point_mass)/dt, applied per step (linear ramp) */
+    int32_t nonfinite_stop;/* 1 (default): a pass with a non-finite radius or velocity ends the
+                              level climb, and a non-finite Levi-Civita state ends the particle's
+                              tau-steps; 0: follow the reference, which keeps climbing (up to
+                              max_subdiv) and stepping (up to max_tau_steps) on such values */
+    int32_t reserved;
 } nsg_params;
 
 typedef struct nsg_ctx nsg_ctx;

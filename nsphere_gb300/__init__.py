@@ -51,7 +51,7 @@ class Params(C.Structure):
         ("lc_rule", C.c_int32), ("lc_alpha", C.c_double), ("lc_radius", C.c_double),
         ("max_tau_steps", C.c_int64), ("sched", C.c_int32), ("carry_aux", C.c_int32),
         ("sort_mode", C.c_int32), ("graph", C.c_int32), ("point_mass", C.c_double),
-        ("point_mass_rate", C.c_double),
+        ("point_mass_rate", C.c_double), ("nonfinite_stop", C.c_int32), ("reserved", C.c_int32),
     ]
 
 

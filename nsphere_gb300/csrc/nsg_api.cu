@@ -334,6 +334,7 @@ int nsg_params_default(nsg_params *p)
     p->carry_aux = 0;
     p->sort_mode = 0;
     p->graph = 1;
+    p->nonfinite_stop = 1;
     return NSG_OK;
 }
 

@@ -54,6 +54,7 @@ struct StepArgs {
     double lc_alpha, lc_radius;
     int N_taumin;
     int64_t max_tau_steps;
+    int nf_stop;                // a non-finite pass ends the climb / the tau-steps (nonfinite_stop)
     DevCounters *ctr;
     uint32_t *q_idx;            // particles that left level 0 (kFreshBit: skipped it)
     double *q_r, *q_v;          // their fine N=1 result (the coarse pass of level 1)
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(512) k_gather_level0(StepArgs a)
             micro_leap<false>(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
             const bool ok = converged<false>(rc, vc, rf, vf, rf, a.tol_r, a.tol_v);
             const bool bad = !(isfinite(rf) && isfinite(vf));
-            done = ok || last || bad;
+            done = ok || last || (bad && a.nf_stop);
             if (done) {
                 double ro, vo;
                 select_out(a.out_type, rc, vc, rf, vf, ro, vo);
@@ -261,7 +262,7 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
                 if (active && kcheck >= kstart) {
                     const bool ok = converged<true>(rC, vC, rF, vF, rF, a.tol_r, a.tol_v);
                     const bool bad = !(isfinite(rF) && isfinite(vF));
-                    if (ok || bad || kcheck == nl) {
+                    if (ok || (bad && a.nf_stop) || kcheck == nl) {
                         if (j == 0) {
                             double ro, vo;
                             select_out(a.out_type, rC, vC, rF, vF, ro, vo);
@@ -446,7 +447,7 @@ __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, doub
                     o.lf = lf;
                 }
                 o.lv = kcheck;
-            } else if (!(isfinite(rF) && isfinite(vF))) {
+            } else if (a.nf_stop && !(isfinite(rF) && isfinite(vF))) {
                 o.r = rF; o.v = vF; o.t = tF;   // non-finite: stop climbing
                 o.lf = lf;
                 o.lv = -1;
@@ -531,7 +532,7 @@ __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
                 }
                 rho = o.r; v = o.v; t = o.t;
                 steps++;
-                if (steps > a.max_tau_steps || !(isfinite(rho) && isfinite(t))) {
+                if (steps > a.max_tau_steps || (a.nf_stop && !(isfinite(rho) && isfinite(t)))) {
                     if (lane == 0) atomicOr(&a.ctr->status, NSG_ST_TAU_CAP);
                     break;
                 }
@@ -725,7 +726,7 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
                     } else {
                         rho = R.r; v = R.v; t = tn;
                         steps++;
-                        if (steps > a.max_tau_steps || !(isfinite(rho) && isfinite(t))) {
+                        if (steps > a.max_tau_steps || (a.nf_stop && !(isfinite(rho) && isfinite(t)))) {
                             if (lane == 0) atomicOr(&a.ctr->status, NSG_ST_TAU_CAP);
                             ro = dmul(rho, rho);
                             vo = v;
@@ -871,6 +872,7 @@ static StepArgs make_args(nsg_ctx *c)
     a.lc_radius = c->p.lc_radius;
     a.N_taumin = c->p.N_taumin;
     a.max_tau_steps = c->p.max_tau_steps;
+    a.nf_stop = c->p.nonfinite_stop != 0;
     a.ctr = c->ctr;
     a.q_idx = c->q_idx[0]; a.q_r = c->q_r[0]; a.q_v = c->q_v[0];
     a.lc_idx = c->lc_idx;

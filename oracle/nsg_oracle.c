@@ -100,9 +100,9 @@ void orc_micro_leap(double r_in, double v_in, double l2, double gnum, double h,
 /* Adaptive full leapfrog step, nsphere.c:1648-1735.  N = 1, 2, 4, ... <= max_subdiv;
  * accepts when both relative coarse/fine differences are below tolerance.
  * *level receives log2(N) of the accepted level, or -1 when no level converged. */
-void orc_adaptive_leap(double r_in, double v_in, double ell, double gnum, double h,
-                       double tol_r, double tol_v, int64_t max_subdiv, int out_type,
-                       double *r_out, double *v_out, int *level)
+static void adaptive_leap_nf(double r_in, double v_in, double ell, double gnum, double h,
+                             double tol_r, double tol_v, int64_t max_subdiv, int out_type,
+                             double *r_out, double *v_out, int *level, int nf_stop)
 {
     double l2 = ell * ell;
     double rc = r_in, vc = v_in, rf = r_in, vf = v_in;
@@ -117,6 +117,9 @@ void orc_adaptive_leap(double r_in, double v_in, double ell, double gnum, double
             *level = k;
             goto out;
         }
+        /* the build's bounded-work rule (nonfinite_stop): a non-finite pass ends the
+         * climb; the reference keeps climbing to max_subdiv */
+        if (nf_stop && !(isfinite(rf) && isfinite(vf))) break;
         N *= 2;
         k++;
     }
@@ -160,7 +163,7 @@ static void micro_lc(double rho_in, double v_in, double t_in, int64_t subSteps,
 static int tau_step_lc(double rho_in, double v_in, double t_in, double h_guess,
                        double tol_r, double tol_v, int64_t max_subdiv, double gnum,
                        double l2, int out_type,
-                       double *rho_out, double *v_out, double *t_out)
+                       double *rho_out, double *v_out, double *t_out, int nf_stop)
 {
     int64_t N = 1;
     int k = 0;
@@ -185,6 +188,10 @@ static int tau_step_lc(double rho_in, double v_in, double t_in, double h_guess,
             }
             return k;
         }
+        if (nf_stop && !(isfinite(rF) && isfinite(vF))) {   /* bounded-work rule */
+            *rho_out = rF; *v_out = vF; *t_out = tF;
+            return -1;
+        }
         N *= 2;
         k++;
     }
@@ -196,10 +203,10 @@ static int tau_step_lc(double rho_in, double v_in, double t_in, double h_guess,
  * *level receives the highest accepted tau-step level (-1 if any tau-step fell
  * back), *ntau the number of tau-steps taken.  Returns 1 when the tau-step cap
  * was hit (the reference's stepMax exit), else 0. */
-int orc_adaptive_lc(double r_in, double v_in, double ell, double gnum, double dt,
-                    int N_taumin, double tol_r, double tol_v, int64_t max_subdiv,
-                    int out_type, int64_t max_tau_steps,
-                    double *r_out, double *v_out, int *level, int64_t *ntau)
+static int adaptive_lc_nf(double r_in, double v_in, double ell, double gnum, double dt,
+                          int N_taumin, double tol_r, double tol_v, int64_t max_subdiv,
+                          int out_type, int64_t max_tau_steps,
+                          double *r_out, double *v_out, int *level, int64_t *ntau, int nf_stop)
 {
     *level = 0;
     *ntau = 0;
@@ -222,7 +229,7 @@ int orc_adaptive_lc(double r_in, double v_in, double ell, double gnum, double dt
         if (t >= dt) break;
         double rn, vn, tn;
         int lv = tau_step_lc(rho, v, t, dtau, tol_r, tol_v, max_subdiv, gnum, l2,
-                             out_type, &rn, &vn, &tn);
+                             out_type, &rn, &vn, &tn, nf_stop);
         if (lv < 0) lvmax = -1;
         else if (lvmax >= 0 && lv > lvmax) lvmax = lv;
         *ntau = steps + 1;
@@ -237,7 +244,7 @@ int orc_adaptive_lc(double r_in, double v_in, double ell, double gnum, double dt
         }
         rho = rn; v = vn; t = tn;
         steps++;
-        if (steps > max_tau_steps) {
+        if (steps > max_tau_steps || (nf_stop && !(isfinite(rho) && isfinite(t)))) {
             *r_out = rho * rho; *v_out = v;
             *level = lvmax;
             return 1;
@@ -246,6 +253,23 @@ int orc_adaptive_lc(double r_in, double v_in, double ell, double gnum, double dt
     *r_out = rho * rho; *v_out = v;
     *level = lvmax;
     return 0;
+}
+
+/* The per-particle integrators as the reference runs them (no bounded-work rule). */
+void orc_adaptive_leap(double r_in, double v_in, double ell, double gnum, double h,
+                       double tol_r, double tol_v, int64_t max_subdiv, int out_type,
+                       double *r_out, double *v_out, int *level)
+{
+    adaptive_leap_nf(r_in, v_in, ell, gnum, h, tol_r, tol_v, max_subdiv, out_type, r_out, v_out, level, 0);
+}
+
+int orc_adaptive_lc(double r_in, double v_in, double ell, double gnum, double dt,
+                    int N_taumin, double tol_r, double tol_v, int64_t max_subdiv,
+                    int out_type, int64_t max_tau_steps,
+                    double *r_out, double *v_out, int *level, int64_t *ntau)
+{
+    return adaptive_lc_nf(r_in, v_in, ell, gnum, dt, N_taumin, tol_r, tol_v, max_subdiv, out_type,
+                          max_tau_steps, r_out, v_out, level, ntau, 0);
 }
 
 /* ------------------------------------------------------------------- sort -- */
@@ -327,13 +351,13 @@ int64_t orc_step_adaptive(const orc_params *p, int64_t n, double *r, double *vr,
         int lv;
         if (use_lc(p, i, n, ri, li)) {
             int64_t nt;
-            capped += orc_adaptive_lc(ri, vi, li, gnum, p->dt, p->N_taumin, p->tol_r,
-                                      p->tol_v, p->max_subdiv, p->out_type,
-                                      p->max_tau_steps, &rn, &vn, &lv, &nt);
+            capped += adaptive_lc_nf(ri, vi, li, gnum, p->dt, p->N_taumin, p->tol_r,
+                                     p->tol_v, p->max_subdiv, p->out_type,
+                                     p->max_tau_steps, &rn, &vn, &lv, &nt, p->nonfinite_stop);
             lv = (lv < 0) ? 99 : 100 + lv;
         } else {
-            orc_adaptive_leap(ri, vi, li, gnum, p->dt, p->tol_r, p->tol_v,
-                              p->max_subdiv, p->out_type, &rn, &vn, &lv);
+            adaptive_leap_nf(ri, vi, li, gnum, p->dt, p->tol_r, p->tol_v,
+                             p->max_subdiv, p->out_type, &rn, &vn, &lv, p->nonfinite_stop);
         }
         r[i] = rn;
         vr[i] = vn;
@@ -397,6 +421,7 @@ void orc_params_default(orc_params *p)
     p->lc_radius = 1.0e-3;
     p->max_tau_steps = 100000000;
     p->point_mass = 0.0;
+    p->nonfinite_stop = 1;
 }
 
 int orc_num_threads(void)

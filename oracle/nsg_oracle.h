@@ -16,6 +16,7 @@ typedef struct orc_params {
     double lc_radius;      /* 1e-3 */
     int64_t max_tau_steps; /* tau-step cap (reference 1e8) */
     double point_mass;     /* central point mass added to M_i (not in the reference; 0 = reference) */
+    int nonfinite_stop;    /* 1: a non-finite pass ends the climb / the tau-steps; 0: the reference */
 } orc_params;
 
 void orc_params_default(orc_params *p);

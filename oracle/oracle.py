@@ -20,6 +20,7 @@ class OrcParams(C.Structure):
         ("tol_v", C.c_double), ("max_subdiv", C.c_int64), ("out_type", C.c_int),
         ("N_taumin", C.c_int), ("lc_rule", C.c_int), ("lc_alpha", C.c_double),
         ("lc_radius", C.c_double), ("max_tau_steps", C.c_int64), ("point_mass", C.c_double),
+        ("nonfinite_stop", C.c_int),
     ]
 
 

@@ -214,6 +214,38 @@ def test_point_mass_ramp_matches_oracle(nsg, oracle, method):
     assert gK == pytest.approx(K, rel=1e-12) and gW == pytest.approx(W, rel=1e-12)
 
 
+@pytest.mark.parametrize("nf_stop", [1, 0])
+@pytest.mark.parametrize("lc_rule", [1, 2])
+def test_nonfinite_rule_matches_oracle(nsg, oracle, nf_stop, lc_rule):
+    """A near-radial particle at the centre with a central mass (found in the N = 1e8
+    point-mass run): its Levi-Civita tau-step overflows in the coarse passes.  With
+    nonfinite_stop = 1 the climb ends there (non-finite radius); with 0 it climbs on to
+    the fallback pass as the reference does (finite result).  lc_rule 2 sends the same
+    particle, and one at r = 0, through the leapfrog.  GPU and oracle agree either way."""
+    pm = float.fromhex("0x1.f75104d551d69p-14")
+    n = 2000
+    r, vr, ell, ids = ics.hernquist(n, seed=9)
+    r, vr, ell = r.copy(), vr.copy(), ell.copy()
+    r[0] = float.fromhex("0x1.0aa796db64b39p-19")
+    vr[0] = float.fromhex("-0x1.24c0ac2752822p+3")
+    ell[0] = float.fromhex("0x1.d1834db7f4eddp-20")
+    if lc_rule == 2:
+        r[1] = 0.0
+    kw = dict(dt=5e-4, max_subdiv=128, lc_rule=lc_rule, lc_radius=1e-3, max_tau_steps=2000, point_mass=pm)
+    p = oracle.params(nonfinite_stop=nf_stop, **kw)
+    orr, ov, ol, oid, olv, cap = oracle.step_adaptive(p, r, vr, ell, ids)
+    with _ctx(nsg, nonfinite_stop=nf_stop, **kw) as c:
+        c.upload(r, vr, ell, ids)
+        c.step(1)
+        gr, gv, gl, gid = c.download()
+        glv = c.levels()
+    assert np.array_equal(gid, oid) and np.array_equal(glv, olv)
+    assert np.array_equal(gr, orr, equal_nan=True) and np.array_equal(gv, ov, equal_nan=True)
+    if lc_rule == 1:
+        k = np.flatnonzero(gid == 0)[0]
+        assert np.isnan(gr[k]) == bool(nf_stop)
+
+
 def test_energy_and_gather(nsg, oracle):
     n = 50000
     r, vr, ell, ids = ics.plummer(n, seed=5)

@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--sched", choices=["plain", "learned"], default="plain")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--ab-steps", type=int, default=8, help="steps of the learned/plain comparison (0: skip)")
+    ap.add_argument("--nonfinite-stop", type=int, default=1, help="stress workload: 0 follows the reference on non-finite passes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
@@ -95,11 +96,12 @@ def workload(args, seed_offset=0):
         ell[pick] = rng.uniform(0.0, 1e-4, int(pick.sum()))
         cfg = dict(workload="hernquist_radial_point_mass", n=args.n, profile="hernquist a=1 r<=100 isotropic",
                    radial_fraction=0.2, radial_ell="U[0, 1e-4]", point_mass="0 -> 0.01 over 500 steps",
+                   nonfinite_stop=args.nonfinite_stop,
                    seed=5 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,
                    lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
         state = (r, vr, ell, ids)
         params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000,
-                      point_mass_rate=0.01 / (500 * 5e-4))
+                      point_mass_rate=0.01 / (500 * 5e-4), nonfinite_stop=args.nonfinite_stop)
     else:
         cfg = dict(workload="hernquist_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 isotropic",
                    seed=2 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,

@@ -486,7 +486,9 @@ __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
     else if (lane <= nlev) my_sub = 4 * ((int64_t)1 << (lane - 1)) + 1;
     else if (lane == nlev + 1) my_sub = 4 * ((int64_t)1 << nlev) + 1;
     const int64_t fb_sub = 4 * ((int64_t)1 << nlev) + 1;
-    for (int64_t e = blockIdx.x; e < cnt; e += gridDim.x) {
+    for (;;) {
+        const unsigned e = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(&a.ctr->lc_next, 1u) : 0u, 0);
+        if (e >= cnt) break;
         const uint32_t i = a.lc_idx[e];
         const uint32_t s = a.perm[i];
         const double r_in = a.r_src[s], v_in = a.v_src[s], ell = a.l_src[s];
@@ -559,8 +561,9 @@ struct LcRecord {
     int pad;
 };
 
-// Shared memory of the paired kernel: two tau-step records, the stop flag, each
-// lane's dtau, then two buffers of lc_slots(nlev) radii.
+// Shared memory of the paired kernel (all dynamic, so that the whole opt-in size can
+// be requested): two tau-step records, the stop flag, the particle taken, the
+// termination index, each lane's dtau, then two buffers of lc_slots(nlev) radii.
 __host__ __device__ __forceinline__ size_t lc_pair_smem(int nlev)
 {
     return 2 * sizeof(LcRecord) + 16 + 32 * sizeof(double) + 2 * (size_t)lc_slots(nlev) * sizeof(double);
@@ -592,6 +595,7 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
     extern __shared__ __align__(16) unsigned char lc_sm[];
     LcRecord *rec = reinterpret_cast<LcRecord *>(lc_sm);
     volatile int *stop = reinterpret_cast<volatile int *>(lc_sm + 2 * sizeof(LcRecord));
+    volatile unsigned *take = reinterpret_cast<volatile unsigned *>(lc_sm + 2 * sizeof(LcRecord) + 4);
     volatile long long *term_at = reinterpret_cast<volatile long long *>(lc_sm + 2 * sizeof(LcRecord) + 8);
     double *dtau_sm = reinterpret_cast<double *>(lc_sm + 2 * sizeof(LcRecord) + 16);
     double *xbuf = dtau_sm + 32;
@@ -609,11 +613,15 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
     else if (role == nlev + 1) my_sub = 4 * ((int64_t)1 << nlev) + 1;
     const int64_t fb_sub = 4 * ((int64_t)1 << nlev) + 1;
     const int64_t off = my_sub ? lc_slot(role, nlev) : 0;
-    for (int64_t e = blockIdx.x; e < cnt; e += gridDim.x) {
+    for (;;) {
+        __syncthreads();                       // the previous particle's buffers are free
+        if (threadIdx.x == 0) *take = atomicAdd(&a.ctr->lc_next, 1u);   // next particle of the list
+        __syncthreads();
+        const unsigned e = *take;
+        if (e >= cnt) break;
         const uint32_t i = a.lc_idx[e];
         const uint32_t s = a.perm[i];
         const double r_in = a.r_src[s], v_in = a.v_src[s], ell = a.l_src[s];
-        __syncthreads();                       // the previous particle's buffers are free
         if (threadIdx.x == 0) { *stop = 0; *term_at = -1; }
         if (r_in < 1.0e-30) {
             if (threadIdx.x == 0) {
@@ -889,7 +897,7 @@ int integrate_adaptive(nsg_ctx *c)
     cudaStream_t s = c->stream;
     cudaError_t e;
     // reset queue counters (qcount[] and lc_count live at the head of DevCounters)
-    e = cudaMemsetAsync(&c->ctr->lc_count, 0, sizeof(unsigned) * (kMaxLevels + 2), s);
+    e = cudaMemsetAsync(&c->ctr->lc_count, 0, sizeof(unsigned) * (kMaxLevels + 3), s);
     if (e != cudaSuccess) return cuda_err(c, e, "memset queue counters");
     const bool lc = (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF);
     // With Levi-Civita particles, their kernel follows the selection directly on the
@@ -910,12 +918,13 @@ int integrate_adaptive(nsg_ctx *c)
         ProfScope ps(c, "levi_civita", 0.0);
         // one block per SM (its shared memory request keeps other blocks off the
         // SM): a warp cannot overlap its own FP64 instructions, and another kernel's
-        // warps on the SM would queue on the same FP64 pipe.  At most a third of the
-        // SMs are taken; further particles wait for a free block.
+        // warps on the SM would queue on the same FP64 pipe.  At most half of the SMs
+        // are taken; each block takes the next particle of the list when it is done
+        // (blocks past the list's end leave at once and free their SM).
         if (a.nlev + 2 <= 16 && lc_pair_smem(a.nlev) <= (size_t)c->lc_smem)
-            k_levi_civita_pair<<<c->num_sms / 3, 64, c->lc_smem, s>>>(a);
+            k_levi_civita_pair<<<c->num_sms / 2, 64, c->lc_smem, s>>>(a);
         else
-            k_levi_civita_lanes<<<c->num_sms / 3, 32, c->lc_smem, s>>>(a);
+            k_levi_civita_lanes<<<c->num_sms / 2, 32, c->lc_smem, s>>>(a);
         c->launches += 1;
     }
     // the scheduler's features and predictions run beside the Levi-Civita chains too

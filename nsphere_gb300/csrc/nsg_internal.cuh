@@ -36,6 +36,7 @@ struct DevCounters {
     unsigned int status;                    // NSG_ST_* bits
     unsigned int lc_count;                  // particles routed to Levi-Civita
     unsigned int qcount[kMaxLevels + 1];    // queue length per leapfrog level
+    unsigned int lc_next;                   // next Levi-Civita list entry a block takes
     unsigned long long level_hist[kStatBins];
     double energy[2];                       // K, W of the last sort
     double point_mass;                      // current central point mass

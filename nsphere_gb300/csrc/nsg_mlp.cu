@@ -688,11 +688,22 @@ using namespace nsg;
 
 extern "C" {
 
+// The network's buffers are also read and written by kernels on the context's
+// streams (collection, learned steps); the calls below touch them with
+// synchronous copies and launches on the default stream, so they first wait for
+// the context's streams to finish.
+static void mlp_quiesce(nsg_ctx *c)
+{
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
+}
+
 int nsg_mlp_num_params(void) { return kParams; }
 
 int nsg_mlp_init(nsg_ctx *c, uint64_t seed)
 {
     if (!c) return set_err(nullptr, NSG_EINVAL, "null context");
+    mlp_quiesce(c);
     if (int rc = mlp_alloc(c)) return rc;
     // He-uniform initial weights from a seeded generator; zero biases and padding
     std::vector<float> w(kParams, 0.f);
@@ -710,6 +721,7 @@ int nsg_mlp_init(nsg_ctx *c, uint64_t seed)
 int nsg_mlp_set_weights(nsg_ctx *c, const float *w, int64_t count)
 {
     if (!c || !w || count != kParams) return set_err(c, NSG_EINVAL, "weights must have nsg_mlp_num_params() floats");
+    mlp_quiesce(c);
     if (int rc = mlp_alloc(c)) return rc;
     MlpDev *m = c->mlp;
     cudaError_t e = cudaMemcpy(m->w, w, kParams * sizeof(float), cudaMemcpyHostToDevice);
@@ -729,6 +741,7 @@ int nsg_mlp_get_weights(nsg_ctx *c, float *w, int64_t count)
 {
     if (!c || !w || count != kParams) return set_err(c, NSG_EINVAL, "weights must have nsg_mlp_num_params() floats");
     if (!c->mlp) return set_err(c, NSG_ESTATE, "no network");
+    mlp_quiesce(c);
     cudaError_t e = cudaMemcpy(w, c->mlp->w, kParams * sizeof(float), cudaMemcpyDeviceToHost);
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "get weights");
 }
@@ -740,6 +753,7 @@ int nsg_mlp_collect(nsg_ctx *c, int nsteps, double keep_level0, int64_t capacity
     if (nsteps < 0 || capacity <= 0 || !(keep_level0 >= 0.0 && keep_level0 <= 1.0))
         return set_err(c, NSG_EINVAL, "bad collect arguments");
     if (c->p.method == NSG_METHOD_KDK) return set_err(c, NSG_EINVAL, "levels exist only for the adaptive methods");
+    mlp_quiesce(c);
     if (int rc = mlp_alloc(c)) return rc;
     MlpDev *m = c->mlp;
     if (m->dcap != capacity) {
@@ -766,6 +780,7 @@ int nsg_mlp_dataset(nsg_ctx *c, int64_t *count, float *X, int8_t *y, int64_t max
 {
     if (!c || !count) return set_err(c, NSG_EINVAL, "null argument");
     if (!c->mlp || !c->mlp->dx) { *count = 0; return NSG_OK; }
+    mlp_quiesce(c);
     unsigned long long h = 0;
     cudaError_t e = cudaMemcpy(&h, c->mlp->dcount, sizeof(h), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_err(c, e, "dataset count");
@@ -797,6 +812,7 @@ int nsg_mlp_grad(nsg_ctx *c, const float *X, const int8_t *y, int64_t nb, const 
 {
     if (!c || !X || !y || nb <= 0 || !cls_w) return set_err(c, NSG_EINVAL, "bad gradient arguments");
     if (!c->mlp || !c->mlp->ready) return set_err(c, NSG_ESTATE, "no network");
+    mlp_quiesce(c);
     for (int64_t k = 0; k < nb; k++)
         if (y[k] < 0 || y[k] >= kOut) return set_err(c, NSG_EINVAL, "class labels must be in 0..7");
     MlpDev *m = c->mlp;
@@ -827,6 +843,7 @@ int nsg_mlp_train(nsg_ctx *c, int epochs, int batch, float lr, uint64_t seed, do
 {
     if (!c || epochs < 0 || batch < 16 || !(lr > 0.f)) return set_err(c, NSG_EINVAL, "bad training arguments");
     if (!c->mlp || !c->mlp->ready) return set_err(c, NSG_ESTATE, "call nsg_mlp_init first");
+    mlp_quiesce(c);
     MlpDev *m = c->mlp;
     int64_t n = 0;
     if (int rc = nsg_mlp_dataset(c, &n, nullptr, nullptr, 0)) return rc;
@@ -881,6 +898,7 @@ int nsg_mlp_predict(nsg_ctx *c, const float *X, int64_t nb, int8_t *cls, float *
 {
     if (!c || !X || nb <= 0 || !cls) return set_err(c, NSG_EINVAL, "bad predict arguments");
     if (!c->mlp || !c->mlp->ready) return set_err(c, NSG_ESTATE, "no network");
+    mlp_quiesce(c);
     float *d_X = nullptr, *d_l = nullptr;
     int8_t *d_c = nullptr;
     cudaError_t e = cudaMalloc((void **)&d_X, (size_t)nb * 16);

@@ -283,7 +283,14 @@ def main():
     E0 = sum(ctx.energy())
     ctx.step(args.warmup)
     torch.cuda.synchronize()
-    l0, _ = ctx.counters()
+    l0, steps0 = ctx.counters()
+    # the state the timed steps start from, so that the per-kernel profile below
+    # replays exactly those steps (download/upload and eager steps leave every bit
+    # as the graph replay does)
+    snap0 = ctx.download()
+    pm0 = p.point_mass
+    for _ in range(steps0):
+        pm0 += p.point_mass_rate * p.dt
 
     def barrier():
         if world > 1:
@@ -308,12 +315,22 @@ def main():
     hist = ctx.level_hist(10)
     status = ctx.status()
 
-    # per-kernel breakdown from the library's own CUDA events (short profiled pass)
-    nprof = 3
+    # per-kernel breakdown from the library's own CUDA events over the same steps as
+    # the timed region, replayed from its starting state
+    nprof = args.steps
+    q = ns.default_params(**params)
+    q.sched = p.sched
+    q.point_mass = pm0
+    ctx.set_params(q)
+    if sizes is None:
+        ctx.upload(*snap0)
+    else:
+        ctx.upload_ensemble(*snap0, sizes)
     ctx.profile(True)
     ctx.step(nprof)
     prof = ctx.profile_read()
     ctx.profile(False)
+    del snap0
 
     # the sort + scan + force pass on its own: fixed-step leapfrog steps of the same
     # state (kick + drift, then bucket sort and the gather that writes the rank force)

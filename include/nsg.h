@@ -210,6 +210,41 @@ int nsg_snapshot_close(nsg_ctx *ctx);
 int nsg_gather(nsg_ctx *ctx, const int32_t *ids, int k, double *r, double *vr,
                double *ell, int32_t *rank);
 
+/* Static potential of the initial halo for the tracking energies.  The reference
+ * tabulates Psi(r) = G M(r)/r + G int_r^inf 4 pi r' rho dr' of its mass-normalised
+ * profile on a 10000-point grid and evaluates a cubic spline of it
+ * (nsphere.c:4575-4592, evaluatespline :8205-8236); here Psi is the closed form of the
+ * same integrals.  NSG_PSI_CORED is the reference's own profile
+ * rho ~ (1 + r^2/a^2)^-3 (massintegrand, nsphere.c:8157-8161; a = RC, r_trunc = 10 RC). */
+#define NSG_PSI_CORED 0
+#define NSG_PSI_PLUMMER 1      /* rho ~ (1 + r^2/a^2)^-5/2 */
+#define NSG_PSI_HERNQUIST 2    /* rho ~ 1 / (r/a (1 + r/a)^3) */
+
+typedef struct nsg_psi {
+    int32_t model;      /* NSG_PSI_* */
+    int32_t reserved;
+    double a;           /* scale radius (RC for the cored profile) */
+    double r_trunc;     /* radius the mass is normalised within (rmax, nsphere.c:4528); <= 0: untruncated */
+    double r_lo, r_hi;  /* table range: r < r_lo is evaluated at r_lo + 1e-10, r > r_hi at r_hi - 1e-10
+                           (the reference's grid is [0, 0.9999 rmax]); r_hi <= 0: no upper clamp */
+} nsg_psi;
+
+/* Device-side trajectory recorder: the per-step tracking of nsphere.c:6384-6450
+ * without a host round trip.  After every step (inside the captured step graph) the
+ * k particles ids[0..k) are looked up through the inverse map and
+ *   r, v_r, ell, E_rel = Psi(r) - (v_r^2 + ell^2/r^2)/2, mu = v_r / sqrt(v_r^2 + ell^2/r^2)
+ * are stored for the next of `capacity` step slots.  The last k_clamped ids are the
+ * low-ell group of :6414-6444, whose radius is first clamped (r < 0 -> 1e-10,
+ * r > r_trunc -> r_trunc) and stored clamped.  G and M are the context's.  Steps after
+ * the buffer is full are counted but not stored.  An id outside [0, n) records NaN.
+ * Opening again replaces the recorder. */
+int nsg_track_open(nsg_ctx *ctx, const int32_t *ids, int k, int k_clamped, const nsg_psi *psi,
+                   int64_t capacity);
+/* Copies the records into out[5][k][capacity] (r, v_r, ell, E_rel, mu; step slot
+ * fastest).  recorded = slots filled, steps_seen = steps since the open. */
+int nsg_track_read(nsg_ctx *ctx, double *out, int64_t *recorded, int64_t *steps_seen);
+int nsg_track_close(nsg_ctx *ctx);
+
 /* Total energy of the resident state, K = sum 1/2 m (v_r^2 + ell^2/r^2) and
  * W = sum m G_num(i)/r_i with the rank enclosed mass of nsphere.c:513.  Sorts the
  * state first (the sort is a total order, so later steps are unaffected). */

@@ -22,6 +22,7 @@ METHOD_KDK, METHOD_ADAPTIVE, METHOD_ADAPTIVE_LC = 2, 3, 5
 LC_RCRIT, LC_RADIUS, LC_OFF = 0, 1, 2
 SCHED_PLAIN, SCHED_LEARNED = 0, 1
 IC_PLUMMER, IC_HERNQUIST = 1, 2
+PSI_CORED, PSI_PLUMMER, PSI_HERNQUIST = 0, 1, 2
 ST_IC_REJECT = 0x20
 ST_NAN, ST_TAU_CAP, ST_NOT_CONVERGED, ST_SORT_FALLBACK, ST_QUEUE = 0x1, 0x2, 0x4, 0x8, 0x10
 
@@ -38,7 +39,7 @@ EXPORTS = [
     "nsg_mlp_collect", "nsg_mlp_dataset", "nsg_mlp_train", "nsg_mlp_grad", "nsg_mlp_predict",
     "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc", "nsg_probe_latency",
     "nsg_write_init", "nsg_read_init", "nsg_snapshot_open", "nsg_snapshot", "nsg_snapshot_close",
-    "nsg_generate", "nsg_potential",
+    "nsg_generate", "nsg_potential", "nsg_track_open", "nsg_track_read", "nsg_track_close",
 ]
 
 
@@ -53,6 +54,18 @@ class Params(C.Structure):
         ("sort_mode", C.c_int32), ("graph", C.c_int32), ("point_mass", C.c_double),
         ("point_mass_rate", C.c_double), ("nonfinite_stop", C.c_int32), ("reserved", C.c_int32),
     ]
+
+
+class Psi(C.Structure):
+    """Mirror of ``nsg_psi`` (include/nsg.h): the static halo potential of tracking."""
+    _fields_ = [("model", C.c_int32), ("reserved", C.c_int32), ("a", C.c_double),
+                ("r_trunc", C.c_double), ("r_lo", C.c_double), ("r_hi", C.c_double)]
+
+
+def reference_psi(rc: float = 100.0) -> Psi:
+    """The reference's own halo (nsphere.c:366, 4528-4592): cored profile with core
+    radius RC, mass normalised within 10 RC, tabulated on [0, 0.9999 * 10 RC]."""
+    return Psi(PSI_CORED, 0, rc, 10.0 * rc, 0.0, 9999.0 / 10000.0 * 10.0 * rc)
 
 
 class KernelStat(C.Structure):
@@ -122,6 +135,9 @@ def lib() -> C.CDLL:
         "nsg_snapshot_open": [P, C.c_char_p, C.c_int],
         "nsg_snapshot": [P],
         "nsg_snapshot_close": [P],
+        "nsg_track_open": [P, P, C.c_int, C.c_int, C.POINTER(Psi), I64],
+        "nsg_track_read": [P, P, C.POINTER(I64), C.POINTER(I64)],
+        "nsg_track_close": [P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -366,6 +382,24 @@ class Context:
 
     def snapshot_close(self):
         self._check(self._L.nsg_snapshot_close(self._h))
+
+    def track_open(self, ids, psi: Psi, capacity: int, k_clamped: int = 0):
+        """Records r, v_r, ell, E_rel, mu of the particles `ids` after every step on
+        the GPU (the reference's tracking, nsphere.c:6384-6450)."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        self._track_k, self._track_cap = len(ids), int(capacity)
+        self._check(self._L.nsg_track_open(self._h, _ptr(ids), len(ids), int(k_clamped), C.byref(psi),
+                                           int(capacity)))
+
+    def track_read(self):
+        """(records[5, k, recorded], steps_seen): r, v_r, ell, E_rel, mu per step."""
+        out = np.empty((5, self._track_k, self._track_cap))
+        rec, seen = C.c_int64(), C.c_int64()
+        self._check(self._L.nsg_track_read(self._h, _ptr(out), C.byref(rec), C.byref(seen)))
+        return out[:, :, :rec.value], seen.value
+
+    def track_close(self):
+        self._check(self._L.nsg_track_close(self._h))
 
     def tune_get(self):
         """Launch shapes: (gather_level0 threads, its blocks/SM, log2 bucket, level blocks/SM)."""

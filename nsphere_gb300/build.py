@@ -22,7 +22,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]
-NO_FMAD = {"nsg_integrate.cu", "nsg_mlp.cu", "nsg_ics.cu", "nsg_post.cu"}
+NO_FMAD = {"nsg_integrate.cu", "nsg_mlp.cu", "nsg_ics.cu", "nsg_post.cu", "nsg_track.cu"}
 
 
 def _nvcc() -> str:

@@ -388,6 +388,7 @@ void nsg_destroy(nsg_ctx *c)
 {
     if (!c) return;
     snap_close(c);
+    track_free(c);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->side) cudaStreamSynchronize(c->side);
     for (auto ev : c->ev_pool) cudaEventDestroy(ev);
@@ -626,6 +627,7 @@ static int one_step(nsg_ctx *c)
     } else {
         rc = integrate_adaptive(c);
     }
+    if (!rc) rc = track_step(c);
     if (rc) return rc;
     if (c->p.point_mass_rate != 0.0) {
         k_advance_point_mass<<<1, 1, 0, c->stream>>>(c->ctr, c->p.point_mass_rate * c->p.dt);

@@ -46,6 +46,7 @@ struct DevCounters {
 
 struct MlpDev;   // nsg_mlp.cu
 struct SnapWriter;   // nsg_io.cu
+struct TrackDev;     // nsg_track.cu
 
 struct KernelStat {
     std::string name;
@@ -121,6 +122,9 @@ struct nsg_ctx {
 
     // snapshot stream (nsg_io.cu), open between nsg_snapshot_open and _close
     nsg::SnapWriter *snap = nullptr;
+
+    // per-step trajectory recorder (nsg_track.cu), open between nsg_track_open and _close
+    nsg::TrackDev *track = nullptr;
 
     // learned level scheduler (nsg_mlp.cu)
     nsg::MlpDev *mlp = nullptr;
@@ -276,6 +280,8 @@ int begin_upload(nsg_ctx *c, int64_t n);              // size the buffers for a 
 int finish_upload_ids(nsg_ctx *c);                    // ids staged as doubles -> int32, validated
 void build_inv(nsg_ctx *c);                           // inv from the current id order
 void snap_close(nsg_ctx *c);                          // end a snapshot stream (nsg_io.cu)
+int track_step(nsg_ctx *c);                           // record the tracked particles (nsg_track.cu)
+void track_free(nsg_ctx *c);
 int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred, cudaStream_t st);  // predicted level per sorted position
 int mlp_features_sorted(nsg_ctx *c, cudaStream_t st);  // features of the sort (training set)
 int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)

@@ -432,3 +432,305 @@ int orc_num_threads(void)
     return 1;
 #endif
 }
+
+/* ---- tracking energies: nsphere.c:6384-6450 with the closed-form potential of the
+ * reference's tabulated integrals (nsphere.c:4575-4592); same operation order as the
+ * device recorder, each operation rounded once (-ffp-contract=off). ---- */
+static double orc_cored_m(double x)
+{
+    const double u = 1.0 + x * x;
+    return (atan(x) + x * (x * x - 1.0) / (u * u)) / 8.0;
+}
+
+static double orc_cored_mx_over_x(double x)
+{
+    if (x < 1e-3) {
+        const double t = x * x;
+        return t * (1.0 / 3.0 - t * (0.6 - t * (6.0 / 7.0)));
+    }
+    const double u = 1.0 + x * x;
+    return (atan(x) + x * (x * x - 1.0) / (u * u)) / 8.0 / x;
+}
+
+double orc_psi(int model, double a, double r_trunc, double r_lo, double r_hi, double G, double M, double r)
+{
+    if (r < r_lo) r = r_lo + 1e-10;
+    else if (r_hi > 0.0 && r > r_hi) r = r_hi - 1e-10;
+    const double R = r_trunc;
+    if (model == 1) {
+        double m = 1.0;
+        if (R > 0.0) {
+            const double s = R / sqrt(R * R + a * a);
+            m = s * s * s;
+        }
+        return G * M / (m * sqrt(r * r + a * a));
+    }
+    if (model == 2) {
+        double m = 1.0;
+        if (R > 0.0) {
+            const double s = R / (R + a);
+            m = s * s;
+        }
+        return G * M / (m * (r + a));
+    }
+    const double m = R > 0.0 ? orc_cored_m(R / a) : 0.19634954084936207;
+    const double x = r / a, u = 1.0 + x * x;
+    return G * M / (a * m) * (orc_cored_mx_over_x(x) + 0.25 / (u * u));
+}
+
+void orc_track(int model, double a, double r_trunc, double r_lo, double r_hi, double G, double M,
+               int k, int k_clamped, const double *r, const double *vr, const double *ell, double *out)
+{
+    for (int t = 0; t < k; t++) {
+        double rr = r[t];
+        const double v = vr[t], l = ell[t];
+        if (t >= k - k_clamped) {
+            if (rr < 0.0) rr = 0.0000000001;
+            if (r_trunc > 0.0 && rr > r_trunc) rr = r_trunc;
+        }
+        const double w = v * v + (l * l) / (rr * rr);
+        out[t] = rr;
+        out[k + t] = v;
+        out[2 * k + t] = l;
+        out[3 * k + t] = orc_psi(model, a, r_trunc, r_lo, r_hi, G, M, rr) - 0.5 * w;
+        out[4 * k + t] = v / sqrt(w);
+    }
+}
+
+/* ---- per-snapshot post-processing (nsphere.c:7060-7990), sequential restatement ----
+ * Natural cubic spline with c_i = y''_i / 2 (the cspline form of the reference's
+ * interpolation library), coefficients by the Thomas algorithm. */
+static int orc_cspline(int64_t m, const double *x, const double *y, double *c)
+{
+    if (m < 3) return -1;
+    double *cp = (double *)malloc((size_t)m * sizeof(double));
+    double *dp = (double *)malloc((size_t)m * sizeof(double));
+    if (!cp || !dp) { free(cp); free(dp); return -1; }
+    c[0] = 0.0;
+    c[m - 1] = 0.0;
+    for (int64_t i = 1; i <= m - 2; i++) {
+        const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+        const double diag = 2.0 * (h0 + h1);
+        const double rhs = 3.0 * ((y[i + 1] - y[i]) / h1 - (y[i] - y[i - 1]) / h0);
+        const double den = (i == 1) ? diag : diag - h0 * cp[i - 1];
+        cp[i] = h1 / den;
+        dp[i] = (i == 1) ? rhs / den : (rhs - h0 * dp[i - 1]) / den;
+    }
+    c[m - 2] = dp[m - 2];
+    for (int64_t i = m - 3; i >= 1; i--) c[i] = dp[i] - cp[i] * c[i + 1];
+    free(cp);
+    free(dp);
+    return 0;
+}
+
+/* largest i <= m-2 with x[i] <= v (x strictly increasing, x[0] <= v) */
+static int64_t orc_interval(int64_t m, const double *x, double v)
+{
+    int64_t lo = 0, hi = m - 1;
+    while (hi > lo + 1) {
+        const int64_t mid = (lo + hi) / 2;
+        if (x[mid] > v) hi = mid;
+        else lo = mid;
+    }
+    return lo;
+}
+
+static double orc_cspline_eval(int64_t m, const double *x, const double *y, const double *c, double v)
+{
+    const int64_t i = orc_interval(m, x, v);
+    const double h = x[i + 1] - x[i], dx = v - x[i];
+    const double b = (y[i + 1] - y[i]) / h - h * (c[i + 1] + 2.0 * c[i]) / 3.0;
+    const double d = (c[i + 1] - c[i]) / (3.0 * h);
+    return y[i] + dx * (b + dx * (c[i] + dx * d));
+}
+
+/* Smoothed density at each sorted radius (nsphere.c:7281-7686 with the causal
+ * Gaussian convolution the zero-padded FFT of :2901-3104 computes, summed directly).
+ * Returns 0, or -1 when the reference's validation rejects the radii. */
+int orc_density(int64_t n, const double *R, double M, double *rho)
+{
+    const double dM = M / (double)n;
+    /* strictly increasing subsequence and its masses (:7297-7329) */
+    double *Rf = (double *)malloc((size_t)n * sizeof(double));
+    double *Mf = (double *)malloc((size_t)n * sizeof(double));
+    int64_t F = 0;
+    for (int64_t i = 0; i < n; i++) {
+        if (F == 0 || R[i] > Rf[F - 1]) {
+            Rf[F] = R[i];
+            Mf[F] = (double)(i + 1) * dM;
+            F++;
+        }
+    }
+    /* decimation (:7331-7361) */
+    int64_t D = (int64_t)ceil((double)n / 100.0);
+    if (D > 30000) D = 30000;
+    if (D <= 0) D = 1;
+    double *Rd = (double *)malloc((size_t)D * sizeof(double));
+    double *Md = (double *)malloc((size_t)D * sizeof(double));
+    if (F <= D) {
+        D = F;
+        memcpy(Rd, Rf, (size_t)F * sizeof(double));
+        memcpy(Md, Mf, (size_t)F * sizeof(double));
+    } else {
+        const double step = (double)(F - 1) / (double)(D - 1);
+        for (int64_t i = 0; i < D; i++) {
+            int64_t idx = (int64_t)round((double)i * step);
+            if (idx >= F) idx = F - 1;
+            Rd[i] = Rf[idx];
+            Md[i] = Mf[idx];
+        }
+    }
+    free(Rf);
+    free(Mf);
+    if (D < 3 || !(Rd[0] > 0.0) || !(Rd[D - 1] > Rd[0]) || !isfinite(Rd[D - 1])) {
+        free(Rd);
+        free(Md);
+        return -1;
+    }
+    /* log grid (:7376-7413) */
+    const int64_t G = 131072;
+    const double min_r = Rd[0], max_r = Rd[D - 1] * 1.04;
+    const double lmin = log10(min_r), lmax = log10(max_r);
+    const double dlog = (lmax - lmin) / (double)(G - 1);
+    double *lg = (double *)malloc((size_t)G * sizeof(double));
+    double *rg = (double *)malloc((size_t)G * sizeof(double));
+    double *mg = (double *)malloc((size_t)G * sizeof(double));
+    double *dg = (double *)malloc((size_t)G * sizeof(double));
+    double *sm = (double *)malloc((size_t)G * sizeof(double));
+    double *kn = (double *)malloc((size_t)G * sizeof(double));
+    double *cg = (double *)malloc((size_t)G * sizeof(double));
+    double *cd = (double *)malloc((size_t)D * sizeof(double));
+    for (int64_t i = 0; i < G; i++) {
+        lg[i] = lmin + (double)i * dlog;
+        rg[i] = pow(10.0, lg[i]);
+    }
+    for (int64_t i = 1; i < G; i++)
+        if (rg[i] <= rg[i - 1]) rg[i] = rg[i - 1] + 1e-12;
+    for (int64_t i = 1; i < D; i++)
+        if (Rd[i] <= Rd[i - 1]) Rd[i] = Rd[i - 1] + 1e-12;
+    /* M(r) on the grid (:7415-7494) */
+    orc_cspline(D, Rd, Md, cd);
+    for (int64_t i = 0; i < G; i++) {
+        if (rg[i] < Rd[0]) mg[i] = Md[0];
+        else if (rg[i] > Rd[D - 1]) mg[i] = Md[D - 1];
+        else mg[i] = orc_cspline_eval(D, Rd, Md, cd, rg[i]);
+    }
+    /* dM/dr by central differences (:7496-7521) */
+    for (int64_t i = 1; i < G - 1; i++) {
+        const double dr = rg[i + 1] - rg[i - 1];
+        if (dr > 1e-15) dg[i] = (mg[i + 1] - mg[i - 1]) / dr;
+        else dg[i] = (i > 1) ? dg[i - 1] : 0.0;
+        if (dg[i] < 1e-10) dg[i] = 1e-10;
+    }
+    dg[0] = dg[1];
+    dg[G - 1] = dg[G - 2];
+    /* Gaussian smoothing in log r (:7539-7570, :2901-3104) */
+    const double sigma = 0.08 * pow((double)n / 10000.0, -0.40);
+    const double step = lg[1] - lg[0];
+    const double pref = 1.0 / (sigma * sqrt(2.0 * M_PI));
+    double norm = 0.0;
+    int64_t W = 0;
+    for (int64_t m = 0; m < G; m++) {
+        const double x = (double)m * step;
+        kn[m] = pref * exp(-0.5 * (x / sigma) * (x / sigma));
+        norm += kn[m];
+        if (kn[m] > 0.0) W = m;
+    }
+    for (int64_t m = 0; m < G; m++) kn[m] /= norm;
+    for (int64_t i = 0; i < G; i++) {
+        double s = 0.0;
+        const int64_t top = i < W ? i : W;
+        for (int64_t m = 0; m <= top; m++) s += kn[m] * dg[i - m];
+        sm[i] = s < 1e-10 ? 1e-10 : s;
+    }
+    /* back to the particles (:7572-7658) */
+    orc_cspline(G, rg, sm, cg);
+    for (int64_t i = 0; i < n; i++) {
+        const double v = R[i];
+        if (v <= rg[0]) rho[i] = sm[0];
+        else if (v >= rg[G - 1]) rho[i] = sm[G - 1];
+        else rho[i] = orc_cspline_eval(G, rg, sm, cg, v);
+    }
+    free(Rd); free(Md); free(lg); free(rg); free(mg); free(dg); free(sm); free(kn); free(cg); free(cd);
+    return 0;
+}
+
+/* Knots of the Psi_A interpolation (nsphere.c:7752-7768): (0, R_0, ..., R_{n-1}) with
+ * every knot not above its predecessor moved to the predecessor + 1e-5. */
+void orc_psi_knots(int64_t n, const double *R, double *knots)
+{
+    knots[0] = 0.0;
+    for (int64_t i = 1; i <= n; i++) {
+        knots[i] = R[i - 1];
+        if (knots[i] <= knots[i - 1]) knots[i] = knots[i - 1] + 1e-5;
+    }
+}
+
+/* linear interpolation on strictly increasing knots; NaN outside */
+static double orc_linear_eval(int64_t m, const double *x, const double *y, double v)
+{
+    if (!(v >= x[0] && v <= x[m - 1])) return NAN;
+    const int64_t i = orc_interval(m, x, v);
+    const double dx = x[i + 1] - x[i];
+    return y[i] + (v - x[i]) / dx * (y[i + 1] - y[i]);
+}
+
+typedef struct { float rad; int64_t idx; } orc_rad_idx;
+static int orc_cmp_rad(const void *a, const void *b)
+{
+    const orc_rad_idx *p = (const orc_rad_idx *)a, *q = (const orc_rad_idx *)b;
+    if (p->rad < q->rad) return -1;
+    if (p->rad > q->rad) return 1;
+    return (p->idx > q->idx) - (p->idx < q->idx);
+}
+
+int orc_post_snapshot(int64_t n, const float *r, const float *v, const float *l, double G, double M,
+                      int64_t *s_idx, double *s_r, double *s_v, double *s_l, double *s_psi, double *s_E,
+                      double *s_rho, double *u_psi, double *u_E, double *psi0)
+{
+    const double dM = M / (double)n;
+    orc_rad_idx *pa = (orc_rad_idx *)malloc((size_t)n * sizeof(orc_rad_idx));
+    for (int64_t i = 0; i < n; i++) {
+        pa[i].rad = (r[i] != r[i]) ? 0.0f : r[i];
+        pa[i].idx = i;
+    }
+    qsort(pa, (size_t)n, sizeof(orc_rad_idx), orc_cmp_rad);
+    for (int64_t i = 0; i < n; i++) {
+        const int64_t o = pa[i].idx;
+        s_idx[i] = o;
+        s_r[i] = (double)pa[i].rad;
+        s_v[i] = (v[o] != v[o]) ? 0.0 : (double)v[o];
+        s_l[i] = (double)l[o];
+    }
+    free(pa);
+    int rc = orc_density(n, s_r, M, s_rho);
+    /* Psi_A at the sorted radii (:7697-7734) */
+    double *psiA = (double *)malloc((size_t)(n + 1) * sizeof(double));
+    double *kx = (double *)malloc((size_t)(n + 1) * sizeof(double));
+    double *suffix = (double *)malloc((size_t)n * sizeof(double));
+    suffix[n - 1] = 1.0 / s_r[n - 1];
+    for (int64_t j = n - 2; j >= 0; j--) suffix[j] = suffix[j + 1] + 1.0 / s_r[j];
+    double sum = 0.0;
+    for (int64_t j = 0; j < n; j++) sum += 1.0 / s_r[j];
+    *psi0 = G * dM * sum;
+    psiA[0] = *psi0;
+    for (int64_t i = 0; i < n; i++) {
+        const double outer = (i < n - 1) ? dM * suffix[i + 1] : 0.0;
+        psiA[i + 1] = G * (((double)(i + 1) * dM) / s_r[i] + outer);
+    }
+    orc_psi_knots(n, s_r, kx);
+    for (int64_t i = 0; i < n; i++) {
+        const double rr = s_r[i];
+        s_psi[i] = orc_linear_eval(n + 1, kx, psiA, rr);
+        s_E[i] = s_psi[i] - (s_l[i] * s_l[i] / (2.0 * rr * rr)) - 0.5 * s_v[i] * s_v[i];
+    }
+    for (int64_t i = 0; i < n; i++) {
+        const double rr = (double)r[i], vv = (double)v[i], ll = (double)l[i];
+        u_psi[i] = orc_linear_eval(n + 1, kx, psiA, rr);
+        u_E[i] = u_psi[i] - (ll * ll / (2.0 * rr * rr)) - 0.5 * vv * vv;
+    }
+    free(psiA);
+    free(kx);
+    free(suffix);
+    return rc;
+}

@@ -39,4 +39,24 @@ void orc_step_kdk(const orc_params *p, int64_t n, double *r, double *vr, double 
 void orc_energy(const orc_params *p, int64_t n, const double *r, const double *vr,
                 const double *ell, double *K, double *W);
 int orc_num_threads(void);
+/* Static halo potential of the tracking energies (nsphere.c:4575-4592, 8205-8236):
+ * model 0 cored (1+x^2)^-3, 1 Plummer, 2 Hernquist; r_trunc <= 0 untruncated;
+ * r < r_lo is evaluated at r_lo + 1e-10 and r > r_hi (> 0) at r_hi - 1e-10. */
+double orc_psi(int model, double a, double r_trunc, double r_lo, double r_hi, double G, double M, double r);
+/* One step's tracking records (nsphere.c:6384-6450) of k particles given their
+ * r, v_r, ell: out[5][k] = r (clamped for the last k_clamped), v_r, ell, E_rel, mu. */
+void orc_track(int model, double a, double r_trunc, double r_lo, double r_hi, double G, double M,
+               int k, int k_clamped, const double *r, const double *vr, const double *ell, double *out);
+/* Per-snapshot post-processing (nsphere.c:7060-7990).
+ * orc_density: smoothed density at each of n sorted radii whose enclosed masses are
+ * (i+1) M/n (returns 0, or -1 when the radii are rejected).
+ * orc_psi_knots: the n+1 knots of the Psi_A interpolation.
+ * orc_post_snapshot: the rank-file quantities of float records r, v, ell in record
+ * order -- sorted by (r, record index): s_idx, s_r, s_v, s_l, s_psi, s_E, s_rho;
+ * record order: u_psi, u_E -- with Psi_A(0) in psi0 (returns orc_density's status). */
+int orc_density(int64_t n, const double *R, double M, double *rho);
+void orc_psi_knots(int64_t n, const double *R, double *knots);
+int orc_post_snapshot(int64_t n, const float *r, const float *v, const float *l, double G, double M,
+                      int64_t *s_idx, double *s_r, double *s_v, double *s_l, double *s_psi, double *s_E,
+                      double *s_rho, double *u_psi, double *u_E, double *psi0);
 #endif

@@ -50,6 +50,9 @@ class Oracle:
                                         C.c_void_p, C.c_void_p]
         L.orc_step_adaptive.restype = I64
         L.orc_step_kdk.argtypes = [C.POINTER(OrcParams), I64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_psi.argtypes = [I, D, D, D, D, D, D, D]
+        L.orc_psi.restype = D
+        L.orc_track.argtypes = [I, D, D, D, D, D, D, I, I, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_energy.argtypes = [C.POINTER(OrcParams), I64, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.POINTER(D), C.POINTER(D)]
         L.orc_num_threads.restype = I
@@ -106,6 +109,17 @@ class Oracle:
 
     def num_threads(self):
         return self.L.orc_num_threads()
+
+    def psi(self, model, a, r_trunc, r_lo, r_hi, r, G=1.0, M=1.0):
+        return self.L.orc_psi(model, a, r_trunc, r_lo, r_hi, G, M, float(r))
+
+    def track(self, model, a, r_trunc, r_lo, r_hi, r, vr, ell, k_clamped=0, G=1.0, M=1.0):
+        """(5, k) records r, v_r, ell, E_rel, mu of one step."""
+        r, vr, ell = (np.ascontiguousarray(x, dtype=np.float64) for x in (r, vr, ell))
+        k = len(r)
+        out = np.empty((5, k))
+        self.L.orc_track(model, a, r_trunc, r_lo, r_hi, G, M, k, k_clamped, _p(r), _p(vr), _p(ell), _p(out))
+        return out
 
 
 class Reference:

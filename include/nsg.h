@@ -187,6 +187,37 @@ int nsg_generate(nsg_ctx *ctx, int model, int64_t n, uint64_t seed, double r_max
  * so values agree with the reference's sequential sums to rounding. */
 int nsg_potential(nsg_ctx *ctx, double *psi, double *E, double *psi0);
 
+/* Records of the reference's Rank files, written with fprintf_bin (nsphere.c:2550-2588:
+ * %d as int32, %f as float), Rank_Mass_Rad_VRad_sorted_t*.dat (nsphere.c:7966-7983)
+ * and Rank_Mass_Rad_VRad_unsorted_t*.dat (:7930-7945). */
+typedef struct nsg_rank_sorted {
+    int32_t rank; float mass, r, vr, psi, E, ell, rho;
+} nsg_rank_sorted;
+typedef struct nsg_rank_unsorted {
+    int32_t rank; float mass, r, vr, psi, E, ell;
+} nsg_rank_unsorted;
+
+/* Per-snapshot post-processing of nsphere.c:7060-7990 on the GPU.  records holds the n
+ * 16-byte snapshot records {int32 rank, float r, v_r, ell} of one all_particle_data
+ * block (nsphere.c:1295-1324, record order = particle order).  The records become the
+ * context's resident state (NaN r and v_r read as 0, :7112-7119; ids = record index)
+ * and are sorted by (r, record index); the reference's qsort leaves the order of equal
+ * radii unspecified.  Outputs (host, either may be NULL): sorted_out[n] -- sorted
+ * position, M = (i+1) M_total/n, r, v_r, Psi_A, E, ell and the smoothed density of
+ * :7281-7686 -- and unsorted_out[n] in record order; *psi0 = Psi_A(0).
+ *   Psi_A at the sorted radii are the knots of a linear interpolation evaluated at
+ *   every radius, with the knots 0, r_0, ..., r_{n-1} made strictly increasing by
+ *   moving each knot not above its predecessor to the predecessor + 1e-5 (:7752-7768).
+ *   The density: M(r) of the strictly increasing radii, decimated to
+ *   min(ceil(n/100), 30000) points, natural cubic spline onto 131072 log-spaced radii,
+ *   dM/dr by central differences (floor 1e-10), smoothed in log r by the normalised
+ *   one-sided Gaussian of width 0.08 (n/1e4)^-0.4 that the reference's zero-padded FFT
+ *   convolution applies (:2901-3104; summed directly here), and splined back to the
+ *   particles.  NSG_EINVAL when the density is undefined (fewer than 3 distinct
+ *   radii after decimation, or a smallest radius <= 0). */
+int nsg_post_snapshot(nsg_ctx *ctx, const void *records, int64_t n, nsg_rank_sorted *sorted_out,
+                      nsg_rank_unsorted *unsorted_out, double *psi0);
+
 /* The initial-conditions file of write_initial_conditions / read_initial_conditions
  * (nsphere.c:2386-2487): int32 npts, then npts records of five doubles (r, v_r, ell,
  * original index, mu).  nsg_write_init writes the resident state in its current

@@ -40,7 +40,15 @@ EXPORTS = [
     "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc", "nsg_probe_latency",
     "nsg_write_init", "nsg_read_init", "nsg_snapshot_open", "nsg_snapshot", "nsg_snapshot_close",
     "nsg_generate", "nsg_potential", "nsg_track_open", "nsg_track_read", "nsg_track_close",
+    "nsg_post_snapshot",
 ]
+
+# records of the reference's Rank files (nsphere.c:7930-7983), as nsg_rank_sorted /
+# nsg_rank_unsorted in include/nsg.h
+RANK_SORTED = np.dtype([("rank", "<i4"), ("mass", "<f4"), ("r", "<f4"), ("vr", "<f4"), ("psi", "<f4"),
+                        ("E", "<f4"), ("ell", "<f4"), ("rho", "<f4")])
+RANK_UNSORTED = np.dtype([("rank", "<i4"), ("mass", "<f4"), ("r", "<f4"), ("vr", "<f4"), ("psi", "<f4"),
+                          ("E", "<f4"), ("ell", "<f4")])
 
 
 class Params(C.Structure):
@@ -138,6 +146,7 @@ def lib() -> C.CDLL:
         "nsg_track_open": [P, P, C.c_int, C.c_int, C.POINTER(Psi), I64],
         "nsg_track_read": [P, P, C.POINTER(I64), C.POINTER(I64)],
         "nsg_track_close": [P],
+        "nsg_post_snapshot": [P, P, I64, P, P, C.POINTER(D)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -250,7 +259,8 @@ class Context:
         self._check(self._L.nsg_sort(self._h))
 
     def download(self, with_aux: bool = False):
-        n = self.n
+        # the library's own count sizes the arrays it fills
+        n = self.n = self._n_from_ctx()
         r, vr, ell, idd = (np.empty(n) for _ in range(4))
         aux = np.empty(n) if with_aux else None
         self._check(self._L.nsg_download(self._h, _ptr(r), _ptr(vr), _ptr(ell), _ptr(idd), _ptr(aux)))
@@ -276,7 +286,7 @@ class Context:
         return h
 
     def levels(self):
-        lv = np.empty(self.n, dtype=np.int8)
+        lv = np.empty(self._n_from_ctx(), dtype=np.int8)
         self._check(self._L.nsg_levels(self._h, _ptr(lv)))
         return lv
 
@@ -357,8 +367,9 @@ class Context:
 
     def potential(self):
         """(psi, E, psi0) of the sorted resident state (see nsg_potential)."""
-        psi = np.empty(self.n)
-        E = np.empty(self.n)
+        n = self._n_from_ctx()
+        psi = np.empty(n)
+        E = np.empty(n)
         p0 = C.c_double()
         self._check(self._L.nsg_potential(self._h, _ptr(psi), _ptr(E), C.byref(p0)))
         return psi, E, p0.value
@@ -400,6 +411,21 @@ class Context:
 
     def track_close(self):
         self._check(self._L.nsg_track_close(self._h))
+
+    def post_snapshot(self, records):
+        """The reference's per-snapshot post-processing (nsphere.c:7060-7990) of one
+        block of 16-byte snapshot records: (sorted RANK_SORTED records, RANK_UNSORTED
+        records in record order, Psi_A(0)).  The records become the resident state."""
+        rec = np.ascontiguousarray(records)
+        if rec.dtype.itemsize != 16:
+            raise ValueError("snapshot records are 16 bytes")
+        n = len(rec)
+        srt = np.empty(n, dtype=RANK_SORTED)
+        uns = np.empty(n, dtype=RANK_UNSORTED)
+        psi0 = C.c_double()
+        self._check(self._L.nsg_post_snapshot(self._h, _ptr(rec), n, _ptr(srt), _ptr(uns), C.byref(psi0)))
+        self.n = n
+        return srt, uns, psi0.value
 
     def tune_get(self):
         """Launch shapes: (gather_level0 threads, its blocks/SM, log2 bucket, level blocks/SM)."""

@@ -22,7 +22,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]
-NO_FMAD = {"nsg_integrate.cu", "nsg_mlp.cu", "nsg_ics.cu", "nsg_post.cu", "nsg_track.cu"}
+NO_FMAD = {"nsg_integrate.cu", "nsg_mlp.cu", "nsg_ics.cu", "nsg_post.cu", "nsg_track.cu", "nsg_density.cu"}
 
 
 def _nvcc() -> str:
@@ -51,7 +51,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or _needs(obj, [src, *headers]):
             flags = list(NVCC_FLAGS)
             if os.path.basename(src) in NO_FMAD:
-                flags.append("--fmad=false")
+                flags += ["--fmad=false", "-Xcompiler=-ffp-contract=off"]
             jobs.append([nvcc, *ARCH, *flags, "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj])
 
     def run(cmd):

@@ -120,6 +120,25 @@ __global__ void __launch_bounds__(kPostThreads) k_post_energy(const double *__re
     }
 }
 
+// Psi_A at each sorted radius into psi[0..n) (and the energies into E) for a sorted
+// radius array r with velocities v, ell; the total of 1/r goes to *total (device).
+// tile: ceil(n / kPostTile) doubles of scratch.
+int post_psi_sorted(nsg_ctx *c, const double *r, const double *v, const double *l, int64_t n, double *psi,
+                    double *E, double *tile, double *total)
+{
+    const int64_t ntiles = (n + kPostTile - 1) / kPostTile;
+    cudaStream_t s = c->stream;
+    k_post_tile_sums<<<(unsigned)ntiles, kPostThreads, 0, s>>>(r, n, tile);
+    k_post_scan_tiles<<<1, 1024, 0, s>>>(tile, ntiles, total);
+    k_post_energy<<<(unsigned)ntiles, kPostThreads, 0, s>>>(r, v, l, n, tile, c->p.G, c->p.M_total / (double)n,
+                                                            psi, E);
+    c->launches += 3;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "potential");
+}
+
+int64_t post_tiles(int64_t n) { return (n + kPostTile - 1) / kPostTile; }
+
 }  // namespace nsg
 
 using namespace nsg;

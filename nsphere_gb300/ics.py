@@ -182,6 +182,15 @@ def snapshot_records(r, vr, ell, ids):
     return out
 
 
+def write_rank_files(sorted_path, unsorted_path, sorted_records, unsorted_records):
+    """Writes Rank_Mass_Rad_VRad_sorted / _unsorted files as the reference's fprintf_bin
+    does (nsphere.c:2550-2588, 7930-7983): the records back to back, no header."""
+    if sorted_path is not None:
+        np.ascontiguousarray(sorted_records).tofile(sorted_path)
+    if unsorted_path is not None:
+        np.ascontiguousarray(unsorted_records).tofile(unsorted_path)
+
+
 # ---------------------------------------------------------------- counter-based generators
 # The restatement, in numpy, of the GPU generators of nsg_generate (csrc/nsg_ics.cu):
 # the same counter-based draws and the same arithmetic, for the tests.

@@ -53,6 +53,10 @@ class Oracle:
         L.orc_psi.argtypes = [I, D, D, D, D, D, D, D]
         L.orc_psi.restype = D
         L.orc_track.argtypes = [I, D, D, D, D, D, D, I, I, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_density.argtypes = [I64, C.c_void_p, D, C.c_void_p]
+        L.orc_psi_knots.argtypes = [I64, C.c_void_p, C.c_void_p]
+        L.orc_psi_knots.restype = None
+        L.orc_post_snapshot.argtypes = [I64, C.c_void_p, C.c_void_p, C.c_void_p, D, D] + [C.c_void_p] * 10
         L.orc_energy.argtypes = [C.POINTER(OrcParams), I64, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.POINTER(D), C.POINTER(D)]
         L.orc_num_threads.restype = I
@@ -109,6 +113,36 @@ class Oracle:
 
     def num_threads(self):
         return self.L.orc_num_threads()
+
+    def density(self, R, M=1.0):
+        """Smoothed density of the reference's post-processing at sorted radii R."""
+        R = np.ascontiguousarray(R, dtype=np.float64)
+        rho = np.empty(len(R))
+        rc = self.L.orc_density(len(R), _p(R), M, _p(rho))
+        if rc:
+            raise ValueError("density undefined for these radii")
+        return rho
+
+    def psi_knots(self, R):
+        R = np.ascontiguousarray(R, dtype=np.float64)
+        k = np.empty(len(R) + 1)
+        self.L.orc_psi_knots(len(R), _p(R), _p(k))
+        return k
+
+    def post_snapshot(self, r, v, l, G=1.0, M=1.0):
+        """Rank-file quantities of float32 records (doubles before the float output)."""
+        r, v, l = (np.ascontiguousarray(x, dtype=np.float32) for x in (r, v, l))
+        n = len(r)
+        out = {k: np.empty(n) for k in ("s_r", "s_v", "s_l", "s_psi", "s_E", "s_rho", "u_psi", "u_E")}
+        idx = np.empty(n, dtype=np.int64)
+        psi0 = C.c_double()
+        rc = self.L.orc_post_snapshot(n, _p(r), _p(v), _p(l), G, M, _p(idx), _p(out["s_r"]), _p(out["s_v"]),
+                                      _p(out["s_l"]), _p(out["s_psi"]), _p(out["s_E"]), _p(out["s_rho"]),
+                                      _p(out["u_psi"]), _p(out["u_E"]), C.byref(psi0))
+        out["s_idx"] = idx
+        out["psi0"] = psi0.value
+        out["density_ok"] = rc == 0
+        return out
 
     def psi(self, model, a, r_trunc, r_lo, r_hi, r, G=1.0, M=1.0):
         return self.L.orc_psi(model, a, r_trunc, r_lo, r_hi, G, M, float(r))

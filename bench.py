@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--ab-steps", type=int, default=8, help="steps of the learned/plain comparison (0: skip)")
     ap.add_argument("--nonfinite-stop", type=int, default=1, help="stress workload: 0 follows the reference on non-finite passes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--post-runs", type=int, default=3,
+                    help="timed runs of the snapshot post-processing of the final state (0: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -404,6 +406,32 @@ def main():
         dist.all_reduce(et, op=dist.ReduceOp.MAX)
     e2e_value = n * world * args.e2e_steps / (float(et.item()) / 1e3)
 
+    # per-snapshot post-processing (Rank-file records with Psi_A and the smoothed
+    # density) of the final state, through the C ABI from host records to host records
+    post = None
+    if args.post_runs > 0 and sizes is None and world == 1:
+        from nsphere_gb300 import ics
+        recs = ics.snapshot_records(*ctx.download())
+        with ns.Context(ns.default_params(), stream=stream.cuda_stream) as pc:
+            pc.post_snapshot(recs)
+            times = []
+            for _ in range(args.post_runs):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                pc.post_snapshot(recs)
+                times.append(time.perf_counter() - t0)
+        post = {"n": n, "ms": 1e3 * statistics.median(times), "runs": args.post_runs,
+                "h2d_bytes": 16 * n, "d2h_bytes": 60 * n,
+                "note": "nsg_post_snapshot, host records in, host Rank records out (blocking call)"}
+        if not args.no_cpu_baseline:
+            from oracle import build_oracle
+            from oracle.oracle import Oracle
+            build_oracle.build_oracle()
+            t0 = time.perf_counter()
+            Oracle().post_snapshot(recs["r"], recs["v"], recs["l"])
+            post["cpu_baseline"] = {"ms": 1e3 * (time.perf_counter() - t0), "cores": 1, "kind": "port",
+                                    "sample": "the same snapshot, sequential restatement (oracle)"}
+
     if rank == 0:
         peaks = {}
         try:
@@ -462,6 +490,7 @@ def main():
             "level_hist": [int(x) for x in hist],
             "status": status,
             "learned_vs_plain": learned,
+            "post_snapshot": post,
         }
         if not args.no_cpu_baseline and world == 1 and sizes is None:
             line["cpu_baseline"] = cpu_baseline(state, params, args.cpu_seconds)

@@ -253,7 +253,7 @@ static void free_buffers(nsg_ctx *c)
         f(c->r[b]); f(c->vr[b]); f(c->ell[b]); f(c->aux[b]); f(c->id[b]);
         f(c->keys[b]); f(c->vals[b]); f(c->q_idx[b]); f(c->q_r[b]); f(c->q_v[b]);
     }
-    f(c->a0); f(c->inv); f(c->level); f(c->tile_counts); f(c->digit_tot); f(c->lc_idx);
+    f(c->a0); f(c->inv); f(c->level); f(c->tile_counts); f(c->digit_tot); f(c->lc_idx); f(c->lc_early);
     f(c->red_part); f(c->stage_d);
     f(c->split); f(c->bcnt); f(c->boff); f(c->bkey); f(c->bpay);
     f(c->d_seg_start); f(c->d_bbase); f(c->seg_energy);
@@ -280,6 +280,7 @@ static int ensure_capacity(nsg_ctx *c, int64_t n)
     A(c->a0, d8); A(c->inv, d4); A(c->level, (size_t)n);
     A(c->tile_counts, (size_t)ntiles * kRadixBuckets * 4); A(c->digit_tot, kRadixBuckets * 4);
     A(c->lc_idx, d4); A(c->red_part, 2 * kReduceBlocks * 8); A(c->stage_d, d8);
+    A(c->lc_early, (size_t)kLcEarlyCap * 20);
     if (e != cudaSuccess) {
         free_buffers(c);
         return cuda_err(c, e, "device allocation");
@@ -368,6 +369,7 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_lcsel, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->ctr, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMemset(c->ctr, 0, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_ctr, sizeof(DevCounters));
@@ -399,6 +401,7 @@ void nsg_destroy(nsg_ctx *c)
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_lcsel) cudaEventDestroy(c->ev_lcsel);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;

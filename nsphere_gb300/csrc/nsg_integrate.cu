@@ -59,6 +59,7 @@ struct StepArgs {
     uint32_t *q_idx;            // particles that left level 0 (kFreshBit: skipped it)
     double *q_r, *q_v;          // their fine N=1 result (the coarse pass of level 1)
     uint32_t *lc_idx;
+    const uint32_t *lc_src;     // source index of each list entry when listed before the sort, or null
     const int8_t *pred;         // learned schedule: predicted level per position, or null
     Seg seg;                    // halos of an ensemble (ranks and sizes are per halo)
     // Substep sizes of each pass, identical for every particle, computed once on
@@ -287,6 +288,7 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
 // k_gather_level0); runs on the side stream right after the sort.
 __global__ void __launch_bounds__(256) k_lc_select(StepArgs a)
 {
+    if (a.ctr->lc_early_ok) return;   // listed before the sort (k_lc_early_rank)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t s = a.perm[i];
@@ -294,6 +296,58 @@ __global__ void __launch_bounds__(256) k_lc_select(StepArgs a)
         const int slot = warp_append(lc, &a.ctr->lc_count);
         if (lc) a.lc_idx[slot] = (uint32_t)i;
     }
+}
+
+// Levi-Civita list before the sort (fixed-radius rule, one halo).  Every particle
+// whose sort key is below the key of lc_radius precedes all others in the sorted
+// order, so its sorted position is its rank among those particles: they are listed
+// here (one pass over the radii), ranked by k_lc_early_rank, and the Levi-Civita
+// chains start while the sort runs.  More than kLcEarlyCap of them leave
+// lc_early_ok at 0, and k_lc_select makes the list after the sort instead.
+__global__ void __launch_bounds__(256) k_lc_early_collect(StepArgs a, uint64_t kthr, uint64_t *__restrict__ ckey,
+                                                          int32_t *__restrict__ cid, uint32_t *__restrict__ csrc)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = radius_key(a.r_src[s]);
+        const bool cand = k < kthr;
+        const int slot = warp_append(cand, &a.ctr->lc_cand);
+        if (cand && slot < kLcEarlyCap) {
+            ckey[slot] = k;
+            cid[slot] = a.id_src[s];
+            csrc[slot] = (uint32_t)s;
+        }
+    }
+}
+
+// Ranks the candidates by (key, id) -- the sort's order -- and lists the Levi-Civita
+// ones with their sorted position and source index.  One block.
+__global__ void __launch_bounds__(1024) k_lc_early_rank(StepArgs a, const uint64_t *__restrict__ ckey,
+                                                        const int32_t *__restrict__ cid,
+                                                        const uint32_t *__restrict__ csrc, uint32_t *__restrict__ lsrc)
+{
+    __shared__ uint64_t sk[kLcEarlyCap];
+    __shared__ int32_t si[kLcEarlyCap];
+    const unsigned cnt = a.ctr->lc_cand;
+    if (cnt > (unsigned)kLcEarlyCap) return;
+    for (unsigned e = threadIdx.x; e < cnt; e += blockDim.x) {
+        sk[e] = ckey[e];
+        si[e] = cid[e];
+    }
+    __syncthreads();
+    for (unsigned e = threadIdx.x; e < cnt; e += blockDim.x) {
+        const uint64_t k = sk[e];
+        const int32_t id = si[e];
+        unsigned rank = 0;
+        for (unsigned j = 0; j < cnt; j++) rank += (sk[j] < k || (sk[j] == k && si[j] < id)) ? 1u : 0u;
+        const uint32_t s = csrc[e];
+        if (route_lc(a, Local{(int64_t)rank, a.n, 0}, a.r_src[s], a.l_src[s])) {
+            const unsigned slot = atomicAdd(&a.ctr->lc_count, 1u);
+            a.lc_idx[slot] = rank;
+            lsrc[slot] = s;
+        }
+    }
+    if (threadIdx.x == 0) a.ctr->lc_early_ok = 1u;
 }
 
 // Division in the Levi-Civita chains.  FAST: the latency-oriented division, with
@@ -490,7 +544,7 @@ __global__ void __launch_bounds__(32) k_levi_civita_lanes(StepArgs a)
         const unsigned e = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(&a.ctr->lc_next, 1u) : 0u, 0);
         if (e >= cnt) break;
         const uint32_t i = a.lc_idx[e];
-        const uint32_t s = a.perm[i];
+        const uint32_t s = a.lc_src ? a.lc_src[e] : a.perm[i];
         const double r_in = a.r_src[s], v_in = a.v_src[s], ell = a.l_src[s];
         const Local L = local_of(a.seg, i, a.n);
         const double gn = gnum_of<true>(L.i, L.n, a.G, a.M, Mpt);
@@ -620,7 +674,7 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
         const unsigned e = *take;
         if (e >= cnt) break;
         const uint32_t i = a.lc_idx[e];
-        const uint32_t s = a.perm[i];
+        const uint32_t s = a.lc_src ? a.lc_src[e] : a.perm[i];
         const double r_in = a.r_src[s], v_in = a.v_src[s], ell = a.l_src[s];
         if (threadIdx.x == 0) { *stop = 0; *term_at = -1; }
         if (r_in < 1.0e-30) {
@@ -884,28 +938,98 @@ static StepArgs make_args(nsg_ctx *c)
     a.ctr = c->ctr;
     a.q_idx = c->q_idx[0]; a.q_r = c->q_r[0]; a.q_v = c->q_v[0];
     a.lc_idx = c->lc_idx;
+    a.lc_src = nullptr;
     a.pred = nullptr;
     a.seg = seg_table(c);
     return a;
 }
 
+// Levi-Civita chains of the list in `a` on stream st: one block per SM (its shared
+// memory request keeps other blocks off the SM): a warp cannot overlap its own FP64
+// instructions, and another kernel's warps on the SM would queue on the same FP64
+// pipe.  At most half of the SMs are taken; each block takes the next particle of
+// the list when it is done (blocks past the list's end leave at once and free their
+// SM).
+static void launch_levi_civita(nsg_ctx *c, const StepArgs &a, cudaStream_t st)
+{
+    if (a.nlev + 2 <= 16 && lc_pair_smem(a.nlev) <= (size_t)c->lc_smem)
+        k_levi_civita_pair<<<c->num_sms / 2, 64, c->lc_smem, st>>>(a);
+    else
+        k_levi_civita_lanes<<<c->num_sms / 2, 32, c->lc_smem, st>>>(a);
+    c->launches += 1;
+}
+
+static uint64_t radius_key_host(double r)
+{
+    if (r != r) return ~0ull;
+    uint64_t u = 0;
+    if (r != 0.0) memcpy(&u, &r, 8);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
 int integrate_adaptive(nsg_ctx *c)
 {
-    if (int rc = sort_perm(c)) return rc;
+    const bool lc = (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF);
+    // fixed-radius rule, one halo: the Levi-Civita list is made before the sort
+    const bool early = lc && c->p.lc_rule == NSG_LC_RADIUS && c->nseg == 1;
+    if (!early)
+        if (int rc = sort_perm(c)) return rc;
     StepArgs a = make_args(c);
     const bool learned = (c->p.sched == NSG_SCHED_LEARNED) && a.nlev > 1;
     cudaStream_t s = c->stream;
     cudaError_t e;
-    // reset queue counters (qcount[] and lc_count live at the head of DevCounters)
-    e = cudaMemsetAsync(&c->ctr->lc_count, 0, sizeof(unsigned) * (kMaxLevels + 3), s);
+    // reset queue counters (lc_count, qcount[], lc_next, lc_cand, lc_early_ok lead DevCounters)
+    e = cudaMemsetAsync(&c->ctr->lc_count, 0, sizeof(unsigned) * (kMaxLevels + 5), s);
     if (e != cudaSuccess) return cuda_err(c, e, "memset queue counters");
-    const bool lc = (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF);
-    // With Levi-Civita particles, their kernel follows the selection directly on the
-    // main stream and the leapfrog kernels run on the side stream after a
-    // cross-stream wait, which resolves later: the Levi-Civita blocks, each of which
-    // needs a whole SM, are placed before the leapfrog blocks fill the GPU.
+    // With Levi-Civita particles, their kernel is launched on the main stream and the
+    // leapfrog kernels run on the side stream after a cross-stream wait, which
+    // resolves later: the Levi-Civita blocks, each of which needs a whole SM, are
+    // placed before the leapfrog blocks fill the GPU.
     cudaStream_t ls = s;
-    if (lc) {
+    if (early) {
+        // main: list + rank the particles below lc_radius, then their chains;
+        // side: the sort, the leapfrog kernels.  The chains start ~the sort's
+        // duration earlier than after the sort.
+        uint64_t *ckey = reinterpret_cast<uint64_t *>(c->lc_early);
+        int32_t *cid = reinterpret_cast<int32_t *>(c->lc_early + (size_t)kLcEarlyCap * 8);
+        uint32_t *csrc = reinterpret_cast<uint32_t *>(c->lc_early + (size_t)kLcEarlyCap * 12);
+        uint32_t *lsrc = reinterpret_cast<uint32_t *>(c->lc_early + (size_t)kLcEarlyCap * 16);
+        {
+            ProfScope ps(c, "lc_prepass", (double)c->n * 8);
+            k_lc_early_collect<<<grid_for(c, c->n, 256, 4), 256, 0, s>>>(a, radius_key_host(c->p.lc_radius), ckey,
+                                                                          cid, csrc);
+            k_lc_early_rank<<<1, 1024, 0, s>>>(a, ckey, cid, csrc, lsrc);
+            c->launches += 2;
+        }
+        e = cudaEventRecord(c->ev_fork, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+        if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
+        {
+            ProfScope ps(c, "levi_civita", 0.0);
+            StepArgs ae = a;
+            ae.lc_src = lsrc;
+            launch_levi_civita(c, ae, s);
+        }
+        const cudaStream_t keep = c->stream;
+        c->stream = c->side;
+        const int rc = sort_perm(c);
+        c->stream = keep;
+        if (rc) return rc;
+        a.perm = c->perm;
+        ls = c->side;
+        {
+            ProfScope ps(c, "lc_select", (double)c->n * 20, ls);
+            k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, ls>>>(a);   // returns at once unless the list overflowed
+            c->launches += 1;
+        }
+        e = cudaEventRecord(c->ev_lcsel, ls);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_lcsel, 0);
+        if (e != cudaSuccess) return cuda_err(c, e, "levi-civita list event");
+        {
+            ProfScope ps(c, "lc_late", 0.0);
+            launch_levi_civita(c, a, s);   // the list made after the sort; empty otherwise
+        }
+    } else if (lc) {
         {
             ProfScope ps(c, "lc_select", (double)c->n * 20);
             k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, s>>>(a);
@@ -916,16 +1040,7 @@ int integrate_adaptive(nsg_ctx *c)
         if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
         ls = c->side;
         ProfScope ps(c, "levi_civita", 0.0);
-        // one block per SM (its shared memory request keeps other blocks off the
-        // SM): a warp cannot overlap its own FP64 instructions, and another kernel's
-        // warps on the SM would queue on the same FP64 pipe.  At most half of the SMs
-        // are taken; each block takes the next particle of the list when it is done
-        // (blocks past the list's end leave at once and free their SM).
-        if (a.nlev + 2 <= 16 && lc_pair_smem(a.nlev) <= (size_t)c->lc_smem)
-            k_levi_civita_pair<<<c->num_sms / 2, 64, c->lc_smem, s>>>(a);
-        else
-            k_levi_civita_lanes<<<c->num_sms / 2, 32, c->lc_smem, s>>>(a);
-        c->launches += 1;
+        launch_levi_civita(c, a, s);
     }
     // the scheduler's features and predictions run beside the Levi-Civita chains too
     if (learned)

@@ -12,6 +12,7 @@ namespace nsg {
 
 constexpr int kMaxLevels = 64;        // adaptive levels N = 2^k, k < 64
 constexpr int kStatBins = 66;         // level histogram bins held on device
+constexpr int kLcEarlyCap = 4096;     // particles below the Levi-Civita radius listed before the sort
 constexpr int kLevelNotConverged = -1;
 constexpr int kLevelLcBase = 100;     // Levi-Civita particles record 100 + level
 constexpr int kLevelLcFallback = 99;
@@ -37,6 +38,8 @@ struct DevCounters {
     unsigned int lc_count;                  // particles routed to Levi-Civita
     unsigned int qcount[kMaxLevels + 1];    // queue length per leapfrog level
     unsigned int lc_next;                   // next Levi-Civita list entry a block takes
+    unsigned int lc_cand;                   // particles below the Levi-Civita radius (list before the sort)
+    unsigned int lc_early_ok;               // 1: the Levi-Civita list was made before the sort
     unsigned long long level_hist[kStatBins];
     double energy[2];                       // K, W of the last sort
     double point_mass;                      // current central point mass
@@ -61,7 +64,7 @@ struct nsg_ctx {
     nsg_params p{};
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;     // leapfrog kernels beside the Levi-Civita chains
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_lcsel = nullptr;
     bool own_stream = false;
     int device = 0;
     int num_sms = 0;
@@ -112,6 +115,7 @@ struct nsg_ctx {
     uint32_t *q_idx[2] = {nullptr, nullptr};
     double *q_r[2] = {nullptr, nullptr}, *q_v[2] = {nullptr, nullptr};
     uint32_t *lc_idx = nullptr;
+    unsigned char *lc_early = nullptr;   // [kLcEarlyCap] candidate keys, ids, sources; list sources
 
     double *red_part = nullptr;      // [2][kReduceBlocks] energy partials
     nsg::DevCounters *ctr = nullptr; // device counters

@@ -114,6 +114,7 @@ def _adaptive_case(n, seed, lowl=0):
 @pytest.mark.parametrize("lc_rule,lc_radius,dt,msub,out_type", [
     (0, 1e-3, 5e-4, 128, 2),      # reference r_crit rule
     (1, 1e-1, 5e-4, 128, 2),      # fixed radius rule (many Levi-Civita particles)
+    (1, 1.0, 5e-4, 128, 2),       # 5015 below the radius: more than the list before the sort holds
     (0, 1e-3, 5e-3, 1 << 12, 2),  # deeper levels (single-warp Levi-Civita kernel)
     (2, 1e-3, 2e-2, 64, 2),       # leapfrog only, level cap reached
     (1, 3e-2, 5e-4, 128, 0),      # coarse-pass output

@@ -314,7 +314,8 @@ int nsg_probe_fp64(double *dfma_tflops, double *div_hw_gps, double *div_int_gps,
  * integer-pipe division (throughput form); [5] dadd + latency-oriented division;
  * [6] 32-bit integer multiply-add; [7] 64-bit multiply-high; [8] int->float, multiply,
  * float->int; [9] one Levi-Civita substep of the leading warp (split force); [10] the
- * same with a zero gravity numerator.  count = how many to measure (<= 11). */
+ * same with a zero gravity numerator; [11] the same with both force quotients in
+ * every lane (no exchange).  count = how many to measure (<= 12). */
 int nsg_probe_latency(double *cycles, int count);
 
 /* ---- learned level scheduler (no reference counterpart: an addition of this

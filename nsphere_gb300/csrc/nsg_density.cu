@@ -41,7 +41,7 @@ constexpr double kKnotStep = 1e-5;       // knot separation of the Psi_A interpo
 constexpr int kKeepThreads = 256, kKeepItems = 16, kKeepTile = kKeepThreads * kKeepItems;
 constexpr int kChunk = 256, kHalo = 96;  // spline chunks
 constexpr int kConvT = 256;              // smoothing tile (outputs and kernel taps)
-constexpr int kKnotWin = 2048;           // radii staged per window of the knot warp
+constexpr int kKnotWin = 4096;           // radii staged per window of the knot warp
 
 __global__ void k_snap_to_state(const SnapIn *__restrict__ rec, int64_t n, double *__restrict__ r,
                                 double *__restrict__ v, double *__restrict__ l, int32_t *__restrict__ id)
@@ -59,15 +59,47 @@ __global__ void k_snap_to_state(const SnapIn *__restrict__ rec, int64_t n, doubl
 
 // knots K[0..n]: K[0] = 0, K[i] = R[i-1] unless R[i-1] <= K[i-1], then K[i-1] + 1e-5.
 // One warp.  In "free" stretches a knot is its radius and the warp finds the first
-// radius not above its predecessor with one ballot per 32 knots.  In a cascade, knot
+// radius not above its predecessor with one ballot per 128 knots.  In a cascade, knot
 // values are y, y (+) c, (y (+) c) (+) c, ...; while y stays in one binade [2^e, 2^e+1)
 // with ulp u, y (+) c = y + K u with K = c/u rounded to nearest (c/u not a tie), as long
 // as y + (K + 1) u < 2^(e+1).  So the bit pattern of the k-th value is bits(y) + k K and
-// 32 knots are formed at once; the steps that leave the binade, a tie, y <= 0 or a
+// 128 knots are formed at once; the steps that leave the binade, a tie, y <= 0 or a
 // subnormal y take one sequential addition.
+// order-preserving key of a non-NaN double (-0 and +0 equal): integer compares only
+__device__ __forceinline__ unsigned long long knot_key(double x)
+{
+    unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    if ((u << 1) == 0ull) u = 0ull;
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// Stages R[lo .. lo + kKnotWin) (zeros past n) into shared memory with asynchronous
+// copies, all in flight at once.
+__device__ __forceinline__ void knot_window(double *win, const double *__restrict__ R, int64_t n, int64_t lo)
+{
+    const int lane = threadIdx.x;
+    __syncwarp();
+    for (int q = lane; q < kKnotWin; q += 32) {
+        const int64_t j = lo + q;
+        if (j < n) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(win + q);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(R + j) : "memory");
+        } else {
+            win[q] = 0.0;
+        }
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncwarp();
+}
+
+// Each lane handles kKnotPer consecutive knots, so one iteration advances up to
+// 32 kKnotPer knots.
+constexpr int kKnotPer = 4;
+
 __global__ void __launch_bounds__(32) k_psi_knots(const double *__restrict__ R, int64_t n, double *__restrict__ K)
 {
-    __shared__ double win[kKnotWin];
+    __shared__ __align__(16) double win[kKnotWin];
+    constexpr int SPAN = 32 * kKnotPer;
     const int lane = threadIdx.x;
     const unsigned full = 0xffffffffu;
     int64_t wb = -1;                 // R index of win[0]
@@ -75,57 +107,80 @@ __global__ void __launch_bounds__(32) k_psi_knots(const double *__restrict__ R, 
     if (lane == 0) K[0] = 0.0;
     int64_t i = 1;                   // next knot
     bool free_mode = true;
+    // binade of y for the closed form: exponent field, K = c/ulp, first bits above it
+    int cur_e = -1;
+    bool closed = false;
+    unsigned long long Kst = 0, end = 0;
     while (i <= n) {
         const int64_t lo = i >= 2 ? i - 2 : 0;
-        if (wb < 0 || lo < wb || i + 31 > wb + kKnotWin) {
-            __syncwarp();
-            for (int q = lane; q < kKnotWin; q += 32) {
-                const int64_t j = lo + q;
-                win[q] = j < n ? R[j] : 0.0;
-            }
-            __syncwarp();
+        if (wb < 0 || lo < wb || i + SPAN > wb + kKnotWin) {
+            knot_window(win, R, n, lo);
             wb = lo;
         }
-        const int64_t j = i + lane;          // this lane's knot
+        const int m0 = lane * kKnotPer;          // this lane's first offset from i
         if (free_mode) {
-            const bool in = j <= n;
-            const double x = in ? win[j - 1 - wb] : 0.0;
-            const double prev = lane == 0 ? y : win[j - 2 - wb];
-            const unsigned b = __ballot_sync(full, in && x <= prev);
-            const unsigned vin = __ballot_sync(full, in);
-            const int f = b ? __ffs(b) - 1 : 32;
-            if (lane < f && in) K[j] = x;
-            if (!b) {
-                const int last = 31 - __clz(vin);
-                y = __shfl_sync(full, x, last);
-                i += last + 1;
+            // first offset m whose radius is not above its predecessor
+            int mine = SPAN;
+            double xs[kKnotPer];
+#pragma unroll
+            for (int q = 0; q < kKnotPer; q++) {
+                const int64_t j = i + m0 + q;
+                const bool in = j <= n;
+                const double x = in ? win[j - 1 - wb] : 0.0;
+                const double prev = (m0 + q == 0) ? y : win[j - 2 - wb];
+                xs[q] = x;
+                if (mine == SPAN && (!in || knot_key(x) <= knot_key(prev))) mine = in ? m0 + q : -(m0 + q) - 1;
+            }
+            // a negative mark ends the array (no trigger there)
+            const bool hit = mine != SPAN;
+            const unsigned b = __ballot_sync(full, hit);
+            const int fl = b ? __ffs(b) - 1 : 32;
+            const int mm = __shfl_sync(full, mine, fl < 32 ? fl : 0);
+            const int f = fl < 32 ? (mm >= 0 ? mm : -mm - 1) : SPAN;   // offsets before f are plain radii
+            const bool trig = fl < 32 && mm >= 0;
+#pragma unroll
+            for (int q = 0; q < kKnotPer; q++)
+                if (m0 + q < f) K[i + m0 + q] = xs[q];
+            if (!trig) {
+                // every knot up to i + f - 1 is its radius
+                const int64_t last = i + f - 1;           // last knot written (f >= 1 here)
+                y = win[last - 1 - wb];
+                i += f;
             } else {
-                y = __shfl_sync(full, prev, f);
+                // knot i + f starts a cascade from its predecessor's value
+                y = (f == 0) ? y : win[i + f - 2 - wb];
                 i += f;
                 free_mode = false;
             }
             continue;
         }
         const long long bits = __double_as_longlong(y);
-        const int e = (int)(bits >> 52);
-        int L = 0;
-        long long Kst = 0;
-        if (y > 0.0 && e > 0 && e < 2047) {
-            const double q = ldexp(kKnotStep, 1075 - e);    // c / ulp(y), exact
-            if (q < 4503599627370496.0 && q - floor(q) != 0.5) {
-                Kst = (long long)rint(q);
-                const long long end = (long long)(e + 1) << 52;
-                if (Kst == 0) L = 32;
-                else if (end - 2 - bits >= 0) {
-                    const long long room = (end - 2 - bits) / Kst;
-                    L = room > 32 ? 32 : (int)room;
+        const int e = (int)(bits >> 52);     // negative for y < 0
+        if (e != cur_e) {
+            cur_e = e;
+            closed = false;
+            if (bits > 0 && e > 0 && e < 2047) {
+                const double q = ldexp(kKnotStep, 1075 - e);    // c / ulp(y), exact
+                if (q < 4503599627370496.0 && q - floor(q) != 0.5) {
+                    closed = true;
+                    Kst = (unsigned long long)rint(q);
+                    end = (unsigned long long)(e + 1) << 52;
                 }
+            }
+        }
+        int L = 0;
+        if (closed) {
+            const unsigned long long ub = (unsigned long long)bits;
+            if (Kst == 0ull || ub + (unsigned long long)SPAN * Kst + 1ull < end) L = SPAN;
+            else if (end >= ub + 2ull) {
+                const unsigned long long room = (end - 2ull - ub) / Kst;
+                L = room > (unsigned long long)SPAN ? SPAN : (int)room;
             }
         }
         if (L <= 0) {
             const double x = win[i - 1 - wb];
             double knot;
-            if (x <= y) {
+            if (knot_key(x) <= knot_key(y)) {
                 knot = y + kKnotStep;
             } else {
                 knot = x;
@@ -136,24 +191,40 @@ __global__ void __launch_bounds__(32) k_psi_knots(const double *__restrict__ R, 
             i += 1;
             continue;
         }
-        const bool act = lane < L;
-        const bool in = act && j <= n;
-        const double Yl = __longlong_as_double(bits + (long long)lane * Kst);
-        const double x = in ? win[j - 1 - wb] : 0.0;
-        const unsigned sb = __ballot_sync(full, act && (!in || !(x <= Yl)));
-        const int f = sb ? __ffs(sb) - 1 : L;
-        if (lane < f) K[j] = __longlong_as_double(bits + (long long)(lane + 1) * Kst);
+        // offset m < L: the cascade value before knot i+m is bits + m K; it stops at the
+        // first m whose radius is above that value (or past the end)
+        int mine = SPAN;
+        double xs[kKnotPer];
+#pragma unroll
+        for (int q = 0; q < kKnotPer; q++) {
+            const int m = m0 + q;
+            const int64_t j = i + m;
+            const bool act = m < L;
+            const bool in = act && j <= n;
+            const double x = in ? win[j - 1 - wb] : 0.0;
+            xs[q] = x;
+            const unsigned long long ym = (unsigned long long)bits + (unsigned long long)m * Kst;
+            if (mine == SPAN && act && (!in || knot_key(x) > (ym | 0x8000000000000000ull))) mine = m;
+        }
+        const unsigned sb = __ballot_sync(full, mine != SPAN);
+        const int fl = sb ? __ffs(sb) - 1 : 32;
+        const int f = fl < 32 ? __shfl_sync(full, mine, fl) : L;
+#pragma unroll
+        for (int q = 0; q < kKnotPer; q++) {
+            const int m = m0 + q;
+            if (m < f) K[i + m] = __longlong_as_double((long long)((unsigned long long)bits + (unsigned long long)(m + 1) * Kst));
+        }
         if (f < L) {
-            const double xf = __shfl_sync(full, x, f);
             const int64_t jf = i + f;
             if (jf <= n) {
+                const double xf = win[jf - 1 - wb];
                 if (lane == 0) K[jf] = xf;
                 y = xf;
                 free_mode = true;
             }
             i = jf + 1;
         } else {
-            y = __longlong_as_double(bits + (long long)L * Kst);
+            y = __longlong_as_double((long long)((unsigned long long)bits + (unsigned long long)L * Kst));
             i += L;
         }
     }
@@ -355,6 +426,18 @@ __device__ __forceinline__ double cs_eval(const double *x, const double *y, cons
     return y[i] + dx * (b + dx * (c[i] + dx * d));
 }
 
+// b_i, d_i of every interval, the same expressions as cs_eval: the evaluation at
+// many points then needs no division
+__global__ void k_cs_coef(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ c,
+                          int64_t m, double *__restrict__ bo, double *__restrict__ dout)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= m - 1) return;
+    const double h = x[i + 1] - x[i];
+    bo[i] = (y[i + 1] - y[i]) / h - h * (c[i + 1] + 2.0 * c[i]) / 3.0;
+    dout[i] = (c[i + 1] - c[i]) / (3.0 * h);
+}
+
 // largest i <= m-2 with x[i] <= v
 __device__ __forceinline__ int64_t interval(const double *x, int64_t m, double v)
 {
@@ -485,8 +568,8 @@ __global__ void __launch_bounds__(kConvT) k_conv(const double *__restrict__ K, c
 }
 
 __global__ void k_rho(const double *__restrict__ R, int64_t n, const double *__restrict__ rg,
-                      const double *__restrict__ sm, const double *__restrict__ cg, double lmin, double dlog,
-                      double *__restrict__ rho)
+                      const double *__restrict__ sm, const double *__restrict__ cg, const double *__restrict__ bg,
+                      const double *__restrict__ dg, double lmin, double dlog, double *__restrict__ rho)
 {
     const double r0 = rg[0], r1 = rg[kGrid - 1];
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
@@ -498,7 +581,8 @@ __global__ void k_rho(const double *__restrict__ R, int64_t n, const double *__r
         j = j < 0 ? 0 : (j > kGrid - 2 ? kGrid - 2 : j);
         while (j > 0 && rg[j] > v) j--;
         while (j < kGrid - 2 && rg[j + 1] <= v) j++;
-        rho[t] = cs_eval(rg, sm, cg, j, v);
+        const double dx = v - rg[j];
+        rho[t] = sm[j] + dx * (bg[j] + dx * (cg[j] + dx * dg[j]));
     }
 }
 
@@ -660,8 +744,11 @@ static int density(nsg_ctx *c, const double *R, int64_t n, double *rho)
     k_scale_grid<<<gb, 256, 0, s>>>(kn, norm);
     k_conv<<<(unsigned)(kGrid / kConvT), kConvT, 0, s>>>(kn, last, dg, sm);
     k_cspline_chunks<<<(unsigned)((chunks_max + 127) / 128), 128, 0, s>>>(rg, sm, kGrid, cg, scratch);
-    k_rho<<<grid_for(c, n, 256), 256, 0, s>>>(R, n, rg, sm, cg, lmin, dlog, rho);
-    c->launches += 20;
+    // the interval coefficients reuse buffers the smoothing no longer needs
+    double *bgc = kn, *dgc = mg;
+    k_cs_coef<<<gb, 256, 0, s>>>(rg, sm, cg, kGrid, bgc, dgc);
+    k_rho<<<grid_for(c, n, 256), 256, 0, s>>>(R, n, rg, sm, cg, bgc, dgc, lmin, dlog, rho);
+    c->launches += 21;
     e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "density");
 }
@@ -690,41 +777,64 @@ extern "C" int nsg_post_snapshot(nsg_ctx *c, const void *records, int64_t n, nsg
     if (e == cudaSuccess) e = B.get(&rho, (size_t)n);
     if (e == cudaSuccess) e = B.get(&tile, (size_t)post_tiles(n));
     if (e == cudaSuccess) e = B.get(&total, 1);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(rec, records, (size_t)n * sizeof(SnapIn), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_err(c, e, "post-processing buffers");
-    k_snap_to_state<<<grid_for(c, n, 256), 256, 0, s>>>(rec, n, c->r[0], c->vr[0], c->ell[0], c->id[0]);
-    c->launches += 1;
+    {
+        ProfScope ps(c, "post_h2d", (double)n * sizeof(SnapIn));
+        e = cudaMemcpyAsync(rec, records, (size_t)n * sizeof(SnapIn), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return cuda_err(c, e, "post-processing upload");
+    }
+    {
+        ProfScope ps(c, "post_unpack", (double)n * (16 + 28));
+        k_snap_to_state<<<grid_for(c, n, 256), 256, 0, s>>>(rec, n, c->r[0], c->vr[0], c->ell[0], c->id[0]);
+        c->launches += 1;
+    }
     if (int rc = sort_state(c)) return rc;
     const int k = c->cur;
     const double *R = c->r[k], *V = c->vr[k], *L = c->ell[k];
-    if (int rc = density(c, R, n, rho)) return rc;
-    if (int rc = post_psi_sorted(c, R, V, L, n, psiK + 1, Esc, tile, total)) return rc;
+    {
+        ProfScope ps(c, "post_density", (double)n * 24);
+        if (int rc = density(c, R, n, rho)) return rc;
+    }
     const double dM = c->p.M_total / (double)n;
-    k_set_psi0<<<1, 1, 0, s>>>(psiK, total, c->p.G, dM);
-    k_psi_knots<<<1, 32, 0, s>>>(R, n, knots);
-    k_psi_interp<<<grid_for(c, n, 256), 256, 0, s>>>(knots, psiK, n + 1, R, nullptr, n, psiS);
-    k_psi_interp<<<grid_for(c, n, 256), 256, 0, s>>>(knots, psiK, n + 1, nullptr, rec, n, psiU);
-    c->launches += 4;
+    {
+        ProfScope ps(c, "post_psi", (double)n * 40);
+        if (int rc = post_psi_sorted(c, R, V, L, n, psiK + 1, Esc, tile, total)) return rc;
+        k_set_psi0<<<1, 1, 0, s>>>(psiK, total, c->p.G, dM);
+        c->launches += 1;
+    }
+    {
+        ProfScope ps(c, "post_knots", (double)n * 16);
+        k_psi_knots<<<1, 32, 0, s>>>(R, n, knots);
+        c->launches += 1;
+    }
+    {
+        ProfScope ps(c, "post_interp", (double)n * 48);
+        k_psi_interp<<<grid_for(c, n, 256), 256, 0, s>>>(knots, psiK, n + 1, R, nullptr, n, psiS);
+        k_psi_interp<<<grid_for(c, n, 256), 256, 0, s>>>(knots, psiK, n + 1, nullptr, rec, n, psiU);
+        c->launches += 2;
+    }
     nsg_rank_sorted *ds = nullptr;
     nsg_rank_unsorted *du = nullptr;
-    if (sorted_out) {
-        e = B.get(&ds, (size_t)n);
-        if (e == cudaSuccess) {
-            k_pack_sorted<<<grid_for(c, n, 256), 256, 0, s>>>(n, R, V, L, psiS, rho, dM, ds);
-            e = cudaMemcpyAsync(sorted_out, ds, (size_t)n * sizeof(nsg_rank_sorted), cudaMemcpyDeviceToHost, s);
-        }
+    if (sorted_out) e = B.get(&ds, (size_t)n);
+    if (e == cudaSuccess && unsorted_out) e = B.get(&du, (size_t)n);
+    if (e != cudaSuccess) return cuda_err(c, e, "post-processing buffers");
+    {
+        ProfScope ps(c, "post_pack", (double)n * (sorted_out ? 72 : 0) + (double)n * (unsorted_out ? 52 : 0));
+        if (ds) k_pack_sorted<<<grid_for(c, n, 256), 256, 0, s>>>(n, R, V, L, psiS, rho, dM, ds);
+        if (du) k_pack_unsorted<<<grid_for(c, n, 256), 256, 0, s>>>(n, rec, psiU, dM, du);
+        c->launches += (ds ? 1 : 0) + (du ? 1 : 0);
     }
-    if (e == cudaSuccess && unsorted_out) {
-        e = B.get(&du, (size_t)n);
-        if (e == cudaSuccess) {
-            k_pack_unsorted<<<grid_for(c, n, 256), 256, 0, s>>>(n, rec, psiU, dM, du);
+    {
+        ProfScope ps(c, "post_d2h", (double)n * ((ds ? 32 : 0) + (du ? 28 : 0)));
+        if (ds) e = cudaMemcpyAsync(sorted_out, ds, (size_t)n * sizeof(nsg_rank_sorted), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && du)
             e = cudaMemcpyAsync(unsorted_out, du, (size_t)n * sizeof(nsg_rank_unsorted), cudaMemcpyDeviceToHost, s);
-        }
     }
     double h0 = 0.0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h0, psiK, 8, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_err(c, e, "post-processing");
     if (psi0) *psi0 = h0;
+    if (c->profiling) prof_flush(c);
     return NSG_OK;
 }

@@ -386,7 +386,10 @@ __device__ __forceinline__ double lc_force(double rho, double gn, double l2, boo
         const double qo = __shfl_xor_sync(0xffffffffu, q, 16);
         return hi ? dadd(q, qo) : dadd(qo, q);
     }
-    return dadd(lc_div<FAST>(gn, p2, bad), lc_div<FAST>(l2, p4, bad));
+    // both quotients in every lane: the gravity one as soon as rho^2 is known, so
+    // that it runs while rho^4 is formed
+    const double qg = lc_div<FAST>(gn, p2, bad);
+    return dadd(qg, lc_div<FAST>(l2, p4, bad));
 }
 
 struct LcTau {
@@ -439,14 +442,14 @@ __host__ __device__ __forceinline__ int64_t lc_slots(int nlev)
 // after each of its substeps at xs[ss] (its own slots), and the result names the
 // lanes whose times the end time is made of.  A tau-step run past the particle's
 // end is abandoned at the next level check once `abandon` is set (lv = -3).
-template <bool FAST, bool PAIR, bool ZG, typename IT>
+template <bool FAST, bool PAIR, bool ZG, typename IT, bool SPLIT = PAIR>
 __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, double v, double t,
                                              double gn, double l2, double dtau, double hdt,
                                              IT my_sub, IT fb_sub, int nlev, double *xs,
                                              const volatile int *abandon, bool &bad)
 {
     double pr = rho, pv = v, pt = t;
-    double hpf = dmul(hdt, lc_force<FAST, ZG, PAIR>(rho, gn, l2, bad));
+    double hpf = dmul(hdt, lc_force<FAST, ZG, SPLIT>(rho, gn, l2, bad));
     LcTau o{rho, v, t, -2, -1, -1};
     int kcheck = 0;
     IT next_end = 5;                     // substeps after which level kcheck's fine pass ends
@@ -458,7 +461,7 @@ __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, doub
         const double vh = dadd(pv, hpf);
         const double hp = (FAST && PAIR) ? lc_half(pr, bs) : dmul(0.5, pr);
         const double rnx = dadd(pr, dmul(dtau, dmul(hp, vh)));
-        const double hf2 = dmul(hdt, lc_force<FAST, ZG, PAIR>(rnx, gn, l2, bs));
+        const double hf2 = dmul(hdt, lc_force<FAST, ZG, SPLIT>(rnx, gn, l2, bs));
         const double vnx = dadd(vh, hf2);
         if (PAIR) {
             if (act && (threadIdx.x & 16) == 0) xs[ss] = rnx;
@@ -816,7 +819,7 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
 // Cycles per substep of lc_tau_step (fast form, PAIR) in a fallback tau-step that
 // one warp runs alone on an SM: split force (nonzero gravity numerator) and zero
 // gravity.  Synthetic inputs; the tolerance 1e-300 keeps every level from converging.
-template <bool ZG>
+template <bool ZG, bool SPLIT>
 __global__ void __launch_bounds__(32) k_lc_probe(StepArgs a, double gn, long long *cyc, double *out)
 {
     __shared__ double xs[2304];
@@ -834,15 +837,15 @@ __global__ void __launch_bounds__(32) k_lc_probe(StepArgs a, double gn, long lon
     const int64_t off = my_sub ? lc_slot(role, nlev) : 0;
     bool bad = false;
     const long long t0 = clock64();
-    LcTau o = lc_tau_step<true, true, ZG, int>(a, 0.0156, 0.03, 0.0, gn, 5.6e-11, dtau, hdt, my_sub, fb, nlev,
-                                               xs + off, &abandon, bad);
+    LcTau o = lc_tau_step<true, true, ZG, int, SPLIT>(a, 0.0156, 0.03, 0.0, gn, 5.6e-11, dtau, hdt, my_sub, fb,
+                                                      nlev, xs + off, &abandon, bad);
     asm volatile("" : "+d"(o.r), "+d"(o.v));
     const long long t1 = clock64();
     out[lane] = o.r + o.v + o.lv + (bad ? 1.0 : 0.0);
     if (lane == 0) cyc[0] = t1 - t0;
 }
 
-int lc_probe_substep(double *cycles_split, double *cycles_zero_gravity)
+int lc_probe_substep(double *cycles_split, double *cycles_zero_gravity, double *cycles_dual)
 {
     StepArgs a;
     memset(&a, 0, sizeof(a));
@@ -854,17 +857,19 @@ int lc_probe_substep(double *cycles_split, double *cycles_zero_gravity)
     double *out = nullptr;
     cudaError_t e = cudaMalloc((void **)&cyc, sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc((void **)&out, 32 * sizeof(double));
-    for (int zg = 0; zg < 2 && e == cudaSuccess; zg++) {
+    for (int kind = 0; kind < 3 && e == cudaSuccess; kind++) {
         for (int rep = 0; rep < 2 && e == cudaSuccess; rep++) {
-            if (zg) k_lc_probe<true><<<1, 32>>>(a, -0.0, cyc, out);
-            else k_lc_probe<false><<<1, 32>>>(a, -2.4e-7, cyc, out);
+            if (kind == 1) k_lc_probe<true, true><<<1, 32>>>(a, -0.0, cyc, out);
+            else if (kind == 0) k_lc_probe<false, true><<<1, 32>>>(a, -2.4e-7, cyc, out);
+            else k_lc_probe<false, false><<<1, 32>>>(a, -2.4e-7, cyc, out);
             e = cudaDeviceSynchronize();
         }
         long long h = 0;
         if (e == cudaSuccess) e = cudaMemcpy(&h, cyc, sizeof(h), cudaMemcpyDeviceToHost);
         const double v = (double)h / (4 * (1 << a.nlev) + 1);
-        if (zg) *cycles_zero_gravity = v;
-        else *cycles_split = v;
+        if (kind == 1) *cycles_zero_gravity = v;
+        else if (kind == 0) *cycles_split = v;
+        else *cycles_dual = v;
     }
     cudaFree(cyc);
     cudaFree(out);

@@ -295,7 +295,7 @@ int mlp_append_levels(nsg_ctx *c);                    // append (features, accep
 void mlp_free(nsg_ctx *c);
 int bucket_setup(nsg_ctx *c);
 int lc_setup(nsg_ctx *c);            // Levi-Civita kernel attributes
-int lc_probe_substep(double *cycles_split, double *cycles_zero_gravity);
+int lc_probe_substep(double *cycles_split, double *cycles_zero_gravity, double *cycles_dual);
 int launch_gather(nsg_ctx *c, const int32_t *d_ids, int k, double *d_out, int32_t *d_rank);
 int launch_level_hist(nsg_ctx *c);
 int launch_ids_from_double(nsg_ctx *c, const double *d_src, int32_t *d_dst, int64_t n);

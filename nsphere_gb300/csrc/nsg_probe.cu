@@ -93,7 +93,7 @@ extern "C" int nsg_probe_latency(double *cycles, int count)
     long long *cyc = nullptr;
     cudaError_t e = cudaMalloc((void **)&out, 64 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void **)&cyc, sizeof(long long));
-    const int n = count < 11 ? count : 11;
+    const int n = count < 12 ? count : 12;
     for (int k = 0; k < n && e == cudaSuccess; k++) {
         long long h = 0;
         const int it = 1024;
@@ -105,8 +105,8 @@ extern "C" int nsg_probe_latency(double *cycles, int count)
             if (e == cudaSuccess) e = cudaMemcpy(&h, cyc, sizeof(h), cudaMemcpyDeviceToHost);
             cycles[k] = (double)h / it;
         } else {
-            double v[2] = {0.0, 0.0};
-            if (int rc = lc_probe_substep(&v[0], &v[1])) { cudaFree(out); cudaFree(cyc); return rc; }
+            double v[3] = {0.0, 0.0, 0.0};
+            if (int rc = lc_probe_substep(&v[0], &v[1], &v[2])) { cudaFree(out); cudaFree(cyc); return rc; }
             cycles[k] = v[k - 9];
         }
     }

@@ -420,9 +420,16 @@ def main():
                 t0 = time.perf_counter()
                 pc.post_snapshot(recs)
                 times.append(time.perf_counter() - t0)
+            pc.profile(True)
+            pc.post_snapshot(recs)
+            stages = pc.profile_read()
+            pc.profile(False)
         post = {"n": n, "ms": 1e3 * statistics.median(times), "runs": args.post_runs,
                 "h2d_bytes": 16 * n, "d2h_bytes": 60 * n,
-                "note": "nsg_post_snapshot, host records in, host Rank records out (blocking call)"}
+                "stages": [{"name": k["name"], "ms": k["total_ms"], "GBps": (k["bytes"] / k["total_ms"] / 1e6)
+                            if k["total_ms"] > 0 else None} for k in stages],
+                "note": "nsg_post_snapshot, host records in, host Rank records out (blocking call); "
+                        "stages from the library's CUDA events in one further run"}
         if not args.no_cpu_baseline:
             from oracle import build_oracle
             from oracle.oracle import Oracle
@@ -462,6 +469,7 @@ def main():
         sort_ms = sum(kby[k]["total_ms"] for k in sort_names if k in kby) / nprof
         sort_gbs = SORT_PASS_BYTES * n / (sort_ms / 1e3) / 1e9 if sort_ms else None
         lc = by.get("levi_civita")
+        lat = fp64["latency_cycles"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -472,6 +480,13 @@ def main():
             "gpu_launches": int(l1 - l0),
             "roofline": roof,
             "critical_path": {
+                "kernel": "k_levi_civita_pair",
+                "bound": "dependent latency of one serial chain (neither HBM nor tensor)",
+                # one substep: 10 dependent FP64 operations and one latency-form
+                # division; the probe's division entry includes one of the 10
+                "substep_cycles": lat["levi_civita_substep"],
+                "substep_floor_cycles": 9 * lat["fp64_fma"] + lat["div_latency_form"],
+                "latency_frac": (9 * lat["fp64_fma"] + lat["div_latency_form"]) / lat["levi_civita_substep"],
                 "levi_civita_ms": (lc["total_ms"] / lc["launches"]) if lc else 0.0,
                 "main_stream_ms": main_ms,
                 "note": "Levi-Civita particles run as serial chains on a side stream; the step ends "

@@ -489,8 +489,8 @@ def main():
                 "latency_frac": (9 * lat["fp64_fma"] + lat["div_latency_form"]) / lat["levi_civita_substep"],
                 "levi_civita_ms": (lc["total_ms"] / lc["launches"]) if lc else 0.0,
                 "main_stream_ms": main_ms,
-                "note": "Levi-Civita particles run as serial chains on a side stream; the step ends "
-                        "when the longest chain ends",
+                "note": "main_stream_ms: every other kernel of the step (sort, leapfrog levels), which runs "
+                        "beside the Levi-Civita chains; the step ends when the longest chain ends",
                 "fp64_dependent_latency_cycles": {"fma": fp64["fma_latency_cycles"],
                                                   "division": fp64["div_latency_cycles"]}},
             "sort_scan_force": {"ms": sort_ms, "GBps": sort_gbs,

@@ -384,7 +384,7 @@ __device__ __forceinline__ double lc_force(double rho, double gn, double l2, boo
         const bool hi = (threadIdx.x & 16) != 0;
         const double q = lc_div<FAST>(hi ? gn : l2, hi ? p2 : p4, bad);
         const double qo = __shfl_xor_sync(0xffffffffu, q, 16);
-        return hi ? dadd(q, qo) : dadd(qo, q);
+        return dadd(q, qo);   // IEEE addition commutes: both halves get gravity + centrifugal
     }
     // both quotients in every lane: the gravity one as soon as rho^2 is known, so
     // that it runs while rho^4 is formed
@@ -448,14 +448,16 @@ __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, doub
                                              IT my_sub, IT fb_sub, int nlev, double *xs,
                                              const volatile int *abandon, bool &bad)
 {
-    double pr = rho, pv = v, pt = t;
+    double pr = rho, pv = v, pt = t, fr = rho, fv = v;
     double hpf = dmul(hdt, lc_force<FAST, ZG, SPLIT>(rho, gn, l2, bad));
     LcTau o{rho, v, t, -2, -1, -1};
     int kcheck = 0;
     IT next_end = 5;                     // substeps after which level kcheck's fine pass ends
     for (IT ss = 0; o.lv == -2; ss++) {
         // every lane computes (the warp issues each instruction once whatever the
-        // active lanes); a lane whose pass has ended keeps its state
+        // active lanes); the working registers of a lane whose pass has ended run on
+        // unused, and the pass's final state is kept aside (fr, fv), so that no select
+        // sits on the dependent chain
         const bool act = ss < my_sub;
         bool bs = false;
         const double vh = dadd(pv, hpf);
@@ -470,9 +472,13 @@ __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, doub
             const double ptn = dadd(pt, dmul(dtau, dmul(rm, rm)));
             pt = act ? ptn : pt;
         }
-        pr = act ? rnx : pr;
-        pv = act ? vnx : pv;
-        hpf = act ? hf2 : hpf;
+        if (ss + 1 == my_sub) {
+            fr = rnx;
+            fv = vnx;
+        }
+        pr = rnx;
+        pv = vnx;
+        hpf = hf2;
         bad |= act && bs;
         if (kcheck < nlev && ss + 1 == next_end) {
             if (PAIR) {
@@ -481,10 +487,10 @@ __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, doub
                 if (ab) { o.lv = -3; break; }
             }
             const int lf = 1 + kcheck, lcz = kcheck;  // fine(k) lane, coarse(k) lane
-            const double rF = __shfl_sync(0xffffffffu, pr, lf);
-            const double vF = __shfl_sync(0xffffffffu, pv, lf);
-            const double rC = __shfl_sync(0xffffffffu, pr, lcz);
-            const double vC = __shfl_sync(0xffffffffu, pv, lcz);
+            const double rF = __shfl_sync(0xffffffffu, fr, lf);
+            const double vF = __shfl_sync(0xffffffffu, fv, lf);
+            const double rC = __shfl_sync(0xffffffffu, fr, lcz);
+            const double vC = __shfl_sync(0xffffffffu, fv, lcz);
             double tF = 0.0, tC = 0.0;
             if (!PAIR) {
                 tF = __shfl_sync(0xffffffffu, pt, lf);
@@ -513,8 +519,8 @@ __device__ __forceinline__ LcTau lc_tau_step(const StepArgs &a, double rho, doub
             next_end = 4 * ((int64_t)1 << kcheck) + 1;
         }
         if (o.lv == -2 && kcheck >= nlev && ss + 1 == fb_sub) {
-            o.r = __shfl_sync(0xffffffffu, pr, nlev + 1);
-            o.v = __shfl_sync(0xffffffffu, pv, nlev + 1);
+            o.r = __shfl_sync(0xffffffffu, fr, nlev + 1);
+            o.v = __shfl_sync(0xffffffffu, fv, nlev + 1);
             if (!PAIR) o.t = __shfl_sync(0xffffffffu, pt, nlev + 1);
             o.lf = nlev + 1;
             o.lv = -1;

@@ -64,25 +64,26 @@ def parse():
 
 
 def workload(args, seed_offset=0):
+    from nsphere_gb300.replicas import replica_seed
     from nsphere_gb300 import ics
     if args.workload == "kdk":
-        cfg = dict(workload="plummer_kdk_fixed_step", n=args.n, profile="plummer", seed=1 + seed_offset,
+        cfg = dict(workload="plummer_kdk_fixed_step", n=args.n, profile="plummer", seed=replica_seed(1, seed_offset),
                    dt=1e-3, method="fixed-step leapfrog (reference method 2)")
-        state = ics.plummer(args.n, seed=1 + seed_offset)
+        state = ics.plummer(args.n, seed=replica_seed(1, seed_offset))
         params = dict(dt=1e-3, method=2)
     elif args.workload == "ensemble":
-        r, vr, ell, ids, sizes = ics.plummer_ensemble(256, 10_000, 1_000_000, seed=3 + seed_offset)
+        r, vr, ell, ids, sizes = ics.plummer_ensemble(256, 10_000, 1_000_000, seed=replica_seed(3, seed_offset))
         cfg = dict(workload="plummer_ensemble_adaptive_lc", n=int(len(r)), halos=256,
-                   halo_n="log-uniform in [1e4, 1e6]", profile="plummer", seed=3 + seed_offset, dt=1e-3,
+                   halo_n="log-uniform in [1e4, 1e6]", profile="plummer", seed=replica_seed(3, seed_offset), dt=1e-3,
                    max_levels=8, max_subdiv=128, lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
         state = (r, vr, ell, ids, sizes)
         params = dict(dt=1e-3, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
         args.n = int(len(r))
     elif args.workload == "om":
         cfg = dict(workload="hernquist_om_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 osipkov-merritt r_a=1",
-                   seed=4 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,
+                   seed=replica_seed(4, seed_offset), dt=5e-4, max_levels=8, max_subdiv=128,
                    lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
-        state = ics.hernquist(args.n, seed=4 + seed_offset, r_a=1.0)
+        state = ics.hernquist(args.n, seed=replica_seed(4, seed_offset), r_a=1.0)
         params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
     elif args.workload == "stress":
         # Hernquist, 20 % of the particles on near-radial orbits (ell uniform in [0, 1e-4]),
@@ -90,25 +91,25 @@ def workload(args, seed_offset=0):
         # generated on the GPU (nsg_generate): the host generator is slow at 1e8
         import nsphere_gb300 as ns
         with ns.Context(ns.default_params()) as g:
-            g.generate(ns.IC_HERNQUIST, args.n, 5 + seed_offset, 100.0)
+            g.generate(ns.IC_HERNQUIST, args.n, replica_seed(5, seed_offset), 100.0)
             r, vr, ell, ids = g.download()
-        rng = np.random.default_rng(5 + seed_offset)
+        rng = np.random.default_rng(replica_seed(5, seed_offset))
         pick = rng.random(args.n) < 0.2
         ell = ell.copy()
         ell[pick] = rng.uniform(0.0, 1e-4, int(pick.sum()))
         cfg = dict(workload="hernquist_radial_point_mass", n=args.n, profile="hernquist a=1 r<=100 isotropic",
                    radial_fraction=0.2, radial_ell="U[0, 1e-4]", point_mass="0 -> 0.01 over 500 steps",
                    nonfinite_stop=args.nonfinite_stop,
-                   seed=5 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,
+                   seed=replica_seed(5, seed_offset), dt=5e-4, max_levels=8, max_subdiv=128,
                    lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
         state = (r, vr, ell, ids)
         params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000,
                       point_mass_rate=0.01 / (500 * 5e-4), nonfinite_stop=args.nonfinite_stop)
     else:
         cfg = dict(workload="hernquist_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 isotropic",
-                   seed=2 + seed_offset, dt=5e-4, max_levels=8, max_subdiv=128,
+                   seed=replica_seed(2, seed_offset), dt=5e-4, max_levels=8, max_subdiv=128,
                    lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
-        state = ics.hernquist(args.n, seed=2 + seed_offset)
+        state = ics.hernquist(args.n, seed=replica_seed(2, seed_offset))
         params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
     cfg["l2"] = "inputs larger than L2 (state %.0f MB vs 129 MB L2); no flush" % (args.n * 28 / 1e6)
     cfg["sched"] = args.sched
@@ -247,9 +248,8 @@ def run_reference_arm(args, rank, world):
 
 def main():
     args = parse()
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from nsphere_gb300.replicas import job_rate, max_over_ranks, rank_env
+    rank, local, world = rank_env()
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
         return
@@ -309,11 +309,8 @@ def main():
     ms = e0.elapsed_time(e1)
     l1, _ = ctx.counters()
     E1 = sum(ctx.energy())
-    ms_t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
-    value = n * world * args.steps / (ms_max / 1e3)
+    ms_max = max_over_ranks(ms, world, device="cuda")
+    value = job_rate(n * args.steps, world, ms_max)
     hist = ctx.level_hist(10)
     status = ctx.status()
 
@@ -401,10 +398,7 @@ def main():
         ctx._check(lib.nsg_download(ctx.handle, P(o_r), P(o_v), P(o_l), P(o_i), None))
     ee1.record(stream)
     barrier()
-    et = torch.tensor([ee0.elapsed_time(ee1)], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(et, op=dist.ReduceOp.MAX)
-    e2e_value = n * world * args.e2e_steps / (float(et.item()) / 1e3)
+    e2e_value = job_rate(n * args.e2e_steps, world, max_over_ranks(ee0.elapsed_time(ee1), world, device="cuda"))
 
     # per-snapshot post-processing (Rank-file records with Psi_A and the smoothed
     # density) of the final state, through the C ABI from host records to host records

@@ -39,6 +39,10 @@ SORT_PASS_BYTES = 72.0
 # DRAM bytes per particle of one k_gather_level0 launch (read + write), from an ncu capture
 # of that kernel at N = 5e6 (160.6 MB read + 122.2 MB written per launch)
 GATHER_LEVEL0_TRAFFIC = (160.628224e6 + 122.180864e6) / 5e6
+# DRAM bytes of one k_levi_civita_pair launch, from an ncu capture of the Hernquist step
+# at N = 2e6 (62.7 KB read, nothing written back to DRAM during the launch); it does not
+# grow with N -- the launch touches only the Levi-Civita particles
+LC_TRAFFIC_PER_LAUNCH = 62.7e3
 # IEEE double operations per particle that k_gather_level0 issues at level 0
 # (rank numerator 3, start force 5, coarse pass 9, fine pass 16, test 6, Richardson 6, l^2 1)
 LEVEL0_FLOPS = 46.0
@@ -330,6 +334,7 @@ def main():
     prof = ctx.profile_read()
     ctx.profile(False)
     del snap0
+    n_lc = int(np.count_nonzero(ctx.levels() >= 99))   # levels 99 and 100+ mark Levi-Civita particles
 
     # the sort + scan + force pass on its own: fixed-step leapfrog steps of the same
     # state (kick + drift, then bucket sort and the gather that writes the rank force)
@@ -445,25 +450,41 @@ def main():
         kby = {k["name"]: k for k in kprof}
         main_ms = sum(k["total_ms"] for k in prof if k["name"] != "levi_civita") / nprof
         tot = sum(k["total_ms"] for k in prof) or 1.0
-        roof = None
+        bulk = None
         if "gather_level0" in by:
             g = by["gather_level0"]
             per = g["total_ms"] / g["launches"]
             ach = (g["bytes"] / g["launches"]) / (per / 1e3) / 1e9
             flops = LEVEL0_FLOPS * n / (per / 1e3) / 1e12
-            roof = {"bound": "hbm", "kernel": "k_gather_level0", "achieved": ach, "peak": hbm_peak,
+            bulk = {"bound": "hbm", "kernel": "k_gather_level0", "achieved": ach, "peak": hbm_peak,
                     "unit": "GB/s", "frac": ach / hbm_peak, "traffic": GATHER_LEVEL0_TRAFFIC * n,
                     "peak_source": peak_src,
-                    "note": "compute-bound on the FP64 pipe (ncu: 75% FP64 pipe active); "
-                            "FP64 view below",
+                    "note": "the largest kernel beside the chains; compute-bound on the FP64 pipe "
+                            "(ncu: 75% FP64 pipe active); FP64 view below",
                     "fp64": {"achieved_tflops": flops, "peak_tflops": fp64["dfma_tflops"],
                              "frac": flops / fp64["dfma_tflops"],
                              "peak_source": "measured live by nsg_probe_fp64 (FMA = 2 flops)"}}
+        # the dominant kernel: the Levi-Civita chains.  Algorithmic bytes per launch:
+        # each Levi-Civita particle reads r, v_r, ell and its list entry (32 B) and
+        # writes r, v_r and its level (17 B).
+        roof = None
+        lcs = by.get("levi_civita")
+        if lcs:
+            per = lcs["total_ms"] / lcs["launches"]
+            alg = 49.0 * n_lc
+            ach = alg / (per / 1e3) / 1e9
+            roof = {"bound": "hbm", "kernel": "k_levi_civita_pair", "achieved": ach, "peak": hbm_peak,
+                    "unit": "GB/s", "frac": ach / hbm_peak, "traffic": LC_TRAFFIC_PER_LAUNCH,
+                    "peak_source": peak_src, "lc_particles": n_lc,
+                    "note": "neither HBM nor tensor bound: each Levi-Civita particle is one serial "
+                            "chain of dependent FP64 operations; its bound is the dependent latency, "
+                            "latency_frac = floor / measured cycles per substep",
+                    "latency_frac": (9 * lat["fp64_fma"] + lat["div_latency_form"]) / lat["levi_civita_substep"]}
+        lat = fp64["latency_cycles"]
         sort_names = ["bucket_scatter", "bucket_sort", "sort_seed", "sort_radix", "gather_kick"]
         sort_ms = sum(kby[k]["total_ms"] for k in sort_names if k in kby) / nprof
         sort_gbs = SORT_PASS_BYTES * n / (sort_ms / 1e3) / 1e9 if sort_ms else None
         lc = by.get("levi_civita")
-        lat = fp64["latency_cycles"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -473,6 +494,7 @@ def main():
                     "d2h_bytes_per_step": 32 * n},
             "gpu_launches": int(l1 - l0),
             "roofline": roof,
+            "bulk_roofline": bulk,
             "critical_path": {
                 "kernel": "k_levi_civita_pair",
                 "bound": "dependent latency of one serial chain (neither HBM nor tensor)",

@@ -484,6 +484,14 @@ def main():
         sort_names = ["bucket_scatter", "bucket_sort", "sort_seed", "sort_radix", "gather_kick"]
         sort_ms = sum(kby[k]["total_ms"] for k in sort_names if k in kby) / nprof
         sort_gbs = SORT_PASS_BYTES * n / (sort_ms / 1e3) / 1e9 if sort_ms else None
+        if roof is None and sort_gbs:
+            # no Levi-Civita chains (fixed-step leapfrog): the sort + scan + force pass dominates
+            roof = {"bound": "hbm", "kernel": "sort + scan + force pass (k_bucket_scatter, k_bucket_sort, "
+                                              "k_gather_rank_force)",
+                    "achieved": sort_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": sort_gbs / hbm_peak,
+                    "traffic": None, "peak_source": peak_src,
+                    "note": "72 algorithmic bytes per particle; the in-bucket sort is shared-memory and "
+                            "issue bound, the gather FP64-pipe bound"}
         lc = by.get("levi_civita")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -450,6 +450,7 @@ def main():
         kby = {k["name"]: k for k in kprof}
         main_ms = sum(k["total_ms"] for k in prof if k["name"] != "levi_civita") / nprof
         tot = sum(k["total_ms"] for k in prof) or 1.0
+        lat = fp64["latency_cycles"]
         bulk = None
         if "gather_level0" in by:
             g = by["gather_level0"]
@@ -480,7 +481,6 @@ def main():
                             "chain of dependent FP64 operations; its bound is the dependent latency, "
                             "latency_frac = floor / measured cycles per substep",
                     "latency_frac": (9 * lat["fp64_fma"] + lat["div_latency_form"]) / lat["levi_civita_substep"]}
-        lat = fp64["latency_cycles"]
         sort_names = ["bucket_scatter", "bucket_sort", "sort_seed", "sort_radix", "gather_kick"]
         sort_ms = sum(kby[k]["total_ms"] for k in sort_names if k in kby) / nprof
         sort_gbs = SORT_PASS_BYTES * n / (sort_ms / 1e3) / 1e9 if sort_ms else None

@@ -39,9 +39,14 @@ extern "C" {
 /* Integration method: the reference's internal method_select codes. */
 #define NSG_METHOD_KDK 2          /* fixed-step leapfrog, vel half-step (CLI --method 6), nsphere.c:5484-5559 */
 #define NSG_METHOD_ADAPTIVE 3     /* adaptive leapfrog only (CLI --method 3) */
+#define NSG_METHOD_FULL_LC 4      /* adaptive leapfrog + fixed-dtau Levi-Civita leapfrog (CLI --method 2),
+                                     nsphere.c:5661-5745 with doLeviCivitaLeapfrog :1827-1937; its r_crit
+                                     rule has no special case for rank 0 (M_i = 0 there), and the reference
+                                     runs it with tol 1e-8, max_subdiv 4096^2 and N_taumin 1000, which the
+                                     caller sets in the params */
 #define NSG_METHOD_ADAPTIVE_LC 5  /* adaptive leapfrog + adaptive Levi-Civita (CLI --method 1, default), nsphere.c:5775-5838 */
 
-/* Levi-Civita routing rule for NSG_METHOD_ADAPTIVE_LC. */
+/* Levi-Civita routing rule for NSG_METHOD_ADAPTIVE_LC and NSG_METHOD_FULL_LC. */
 #define NSG_LC_RCRIT 0   /* r < alpha * ell^2 / (G M_i), reference rule nsphere.c:5804-5822 */
 #define NSG_LC_RADIUS 1  /* r < lc_radius */
 #define NSG_LC_OFF 2     /* never */

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(_PKG, "libnsg.so")
 NSG_OK = 0
 NSG_EINVAL, NSG_ECUDA, NSG_ENOMEM, NSG_ESTATE, NSG_EIDS, NSG_EDEVICE, NSG_ETIMEOUT = (
     -1, -2, -3, -4, -5, -6, -7)
-METHOD_KDK, METHOD_ADAPTIVE, METHOD_ADAPTIVE_LC = 2, 3, 5
+METHOD_KDK, METHOD_ADAPTIVE, METHOD_FULL_LC, METHOD_ADAPTIVE_LC = 2, 3, 4, 5
 LC_RCRIT, LC_RADIUS, LC_OFF = 0, 1, 2
 SCHED_PLAIN, SCHED_LEARNED = 0, 1
 IC_PLUMMER, IC_HERNQUIST = 1, 2

@@ -299,7 +299,8 @@ static int check_params(nsg_ctx *c, const nsg_params *p)
 {
     if (!p) return set_err(c, NSG_EINVAL, "null params");
     if (!(p->dt > 0.0) || !isfinite(p->dt)) return set_err(c, NSG_EINVAL, "dt must be positive and finite");
-    if (p->method != NSG_METHOD_KDK && p->method != NSG_METHOD_ADAPTIVE && p->method != NSG_METHOD_ADAPTIVE_LC)
+    if (p->method != NSG_METHOD_KDK && p->method != NSG_METHOD_ADAPTIVE && p->method != NSG_METHOD_ADAPTIVE_LC &&
+        p->method != NSG_METHOD_FULL_LC)
         return set_err(c, NSG_EINVAL, "unknown method");
     if (p->max_subdiv < 1) return set_err(c, NSG_EINVAL, "max_subdiv must be >= 1");
     // one warp holds every level of a Levi-Civita tau-step: levels + 2 <= 32 lanes

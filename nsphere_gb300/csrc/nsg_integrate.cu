@@ -114,9 +114,18 @@ __device__ __forceinline__ void select_out(int out_type, double rc, double vc, d
 // Routing of nsphere.c:5804-5822 (alpha rule), or a fixed radius.
 __device__ __forceinline__ bool route_lc(const StepArgs &a, const Local &L, double r, double ell)
 {
-    if (a.method != NSG_METHOD_ADAPTIVE_LC || a.lc_rule == NSG_LC_OFF) return false;
+    if ((a.method != NSG_METHOD_ADAPTIVE_LC && a.method != NSG_METHOD_FULL_LC) || a.lc_rule == NSG_LC_OFF)
+        return false;
     if (a.lc_rule == NSG_LC_RADIUS) return (r > 1.0e-30) && (r < a.lc_radius);
     double r_crit = 0.0;
+    if (a.method == NSG_METHOD_FULL_LC) {
+        // method 4 (nsphere.c:5696-5707): M_i = (i/N) M for every rank, any ell != 0
+        if (ell != 0.0) {
+            const double gravPart = dmul(a.G, dmul(ddiv((double)L.i, (double)L.n), a.M));
+            r_crit = ddiv(dmul(dmul(ell, ell), a.lc_alpha), gravPart);
+        }
+        return (r > 1.0e-30) && (r < r_crit);
+    }
     if (fabs(ell) > 1.0e-30) {
         double M_enc;
         if (L.i == 0) M_enc = dmul(dmul(0.1, ddiv(1.0, (double)L.n)), a.M);
@@ -822,6 +831,85 @@ __global__ void __launch_bounds__(64) k_levi_civita_pair(StepArgs a)
     }
 }
 
+// The Levi-Civita force with every quotient exact: the latency-form divisions, and
+// the FP64 pipe's when one of them does not claim its result.
+__device__ __forceinline__ double lc_force_exact(double rho, double gn, double l2)
+{
+    bool bad = false;
+    const double f = lc_force<true>(rho, gn, l2, bad);
+    if (!bad) return f;
+    return lc_force<false>(rho, gn, l2, bad);
+}
+
+// Method 4's fixed-dtau Levi-Civita leapfrog (doLeviCivitaLeapfrog, nsphere.c:1827-1937):
+// one thread per particle, taken from the list through the atomic counter.  Each
+// substep kicks, drifts rho, kicks and adds dtau rho_mid^2 to the physical time until
+// it reaches dt, then interpolates (alpha = 1 when the substep added no time).  The
+// force at the start of a substep is the one at the end of the previous.
+__global__ void __launch_bounds__(32) k_levi_civita_fixed(StepArgs a)
+{
+    const unsigned cnt = a.ctr->lc_count;
+    if (cnt == 0) return;
+    const double Mpt = a.ctr->point_mass;
+    for (;;) {
+        const unsigned e = atomicAdd(&a.ctr->lc_next, 1u);
+        if (e >= cnt) break;
+        const uint32_t i = a.lc_idx[e];
+        const uint32_t s = a.lc_src ? a.lc_src[e] : a.perm[i];
+        const double r_in = a.r_src[s], v_in = a.v_src[s], ell = a.l_src[s];
+        const Local L = local_of(a.seg, i, a.n);
+        const double gn = gnum_of<true>(L.i, L.n, a.G, a.M, Mpt);
+        const double l2 = dmul(ell, ell);
+        double dtau;
+        if (r_in > 1.0e-30 && a.N_taumin > 0)
+            dtau = __ddiv_rn(a.dt, dmul(dmul(2.0, r_in), (double)a.N_taumin));
+        else
+            dtau = __ddiv_rn(a.dt, 100.0);
+        const double hdt = dmul(0.5, dtau);
+        double rho = sqrt(r_in), v = v_in, t = 0.0, ro = 0.0, vo = 0.0;
+        double f = lc_force_exact(rho, gn, l2);
+        int64_t steps = 0;
+        bool done = false, capped = false;
+        while (!done) {
+            if (t >= a.dt) {
+                ro = dmul(rho, rho);
+                vo = v;
+                break;
+            }
+            const double vh = dadd(v, dmul(hdt, f));
+            const double rn = dadd(rho, dmul(dtau, dmul(dmul(0.5, rho), vh)));
+            const double f2 = lc_force_exact(rn, gn, l2);
+            const double vn = dadd(vh, dmul(hdt, f2));
+            const double rm = dmul(0.5, dadd(rho, rn));
+            const double tn = dadd(t, dmul(dtau, dmul(rm, rm)));
+            if (tn >= a.dt) {
+                double alpha = 1.0;
+                if (fabs(dsub(tn, t)) > 1.0e-30) alpha = __ddiv_rn(dsub(a.dt, t), dsub(tn, t));
+                const double rf = dadd(rho, dmul(alpha, dsub(rn, rho)));
+                ro = dmul(rf, rf);
+                vo = dadd(v, dmul(alpha, dsub(vn, v)));
+                done = true;
+            } else {
+                rho = rn;
+                v = vn;
+                t = tn;
+                f = f2;
+                steps++;
+                if (steps > a.max_tau_steps || (a.nf_stop && !(isfinite(rho) && isfinite(t)))) {
+                    ro = dmul(rho, rho);
+                    vo = v;
+                    capped = true;
+                    done = true;
+                }
+            }
+        }
+        if (capped) atomicOr(&a.ctr->status, NSG_ST_TAU_CAP);
+        a.r_out[i] = ro;
+        a.v_out[i] = vo;
+        a.level[i] = (int8_t)kLevelLcBase;
+    }
+}
+
 // Cycles per substep of lc_tau_step (fast form, PAIR) in a fallback tau-step that
 // one warp runs alone on an SM: split force (nonzero gravity numerator) and zero
 // gravity.  Synthetic inputs; the tolerance 1e-300 keeps every level from converging.
@@ -963,7 +1051,9 @@ static StepArgs make_args(nsg_ctx *c)
 // SM).
 static void launch_levi_civita(nsg_ctx *c, const StepArgs &a, cudaStream_t st)
 {
-    if (a.nlev + 2 <= 16 && lc_pair_smem(a.nlev) <= (size_t)c->lc_smem)
+    if (a.method == NSG_METHOD_FULL_LC)
+        k_levi_civita_fixed<<<c->num_sms, 32, 0, st>>>(a);
+    else if (a.nlev + 2 <= 16 && lc_pair_smem(a.nlev) <= (size_t)c->lc_smem)
         k_levi_civita_pair<<<c->num_sms / 2, 64, c->lc_smem, st>>>(a);
     else
         k_levi_civita_lanes<<<c->num_sms / 2, 32, c->lc_smem, st>>>(a);
@@ -980,7 +1070,8 @@ static uint64_t radius_key_host(double r)
 
 int integrate_adaptive(nsg_ctx *c)
 {
-    const bool lc = (c->p.method == NSG_METHOD_ADAPTIVE_LC && c->p.lc_rule != NSG_LC_OFF);
+    const bool lc = ((c->p.method == NSG_METHOD_ADAPTIVE_LC || c->p.method == NSG_METHOD_FULL_LC) &&
+                     c->p.lc_rule != NSG_LC_OFF);
     // fixed-radius rule, one halo: the Levi-Civita list is made before the sort
     const bool early = lc && c->p.lc_rule == NSG_LC_RADIUS && c->nseg == 1;
     if (!early)

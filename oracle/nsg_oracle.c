@@ -255,6 +255,59 @@ static int adaptive_lc_nf(double r_in, double v_in, double ell, double gnum, dou
     return 0;
 }
 
+/* Fixed-dtau Levi-Civita leapfrog over physical dt, nsphere.c:1827-1937: kick, drift
+ * in rho, kick, t += dtau rho_mid^2, until t reaches dt, then linear interpolation
+ * (alpha = 1 when the last substep added no time).  The force at the start of a
+ * substep is the one at the end of the previous (same operands, same value). */
+static int lc_fixed_nf(double r_in, double v_in, double ell, double gnum, double dt, int N_taumin,
+                       int64_t max_steps, double *r_out, double *v_out, int nf_stop)
+{
+    const double l2 = ell * ell;
+    double rho = sqrt(r_in), v = v_in, t = 0.0;
+    double dtau;
+    if (r_in > 1.0e-30 && N_taumin > 0)
+        dtau = dt / (2.0 * r_in * (double)N_taumin);
+    else
+        dtau = dt / 100.0;
+    int64_t steps = 0;
+    for (;;) {
+        if (t >= dt) break;
+        const double f = acc_lc(rho, gnum, l2);
+        const double vh = v + 0.5 * dtau * f;
+        const double rn = rho + dtau * (0.5 * rho * vh);
+        const double f2 = acc_lc(rn, gnum, l2);
+        const double vn = vh + 0.5 * dtau * f2;
+        const double rm = 0.5 * (rho + rn);
+        const double tn = t + dtau * (rm * rm);
+        if (tn >= dt) {
+            double alpha;
+            if (fabs(tn - t) > 1.0e-30) alpha = (dt - t) / (tn - t);
+            else alpha = 1.0;
+            const double rf = rho + alpha * (rn - rho);
+            const double vf = v + alpha * (vn - v);
+            *r_out = rf * rf;
+            *v_out = vf;
+            return 0;
+        }
+        rho = rn; v = vn; t = tn;
+        steps++;
+        if (steps > max_steps || (nf_stop && !(isfinite(rho) && isfinite(t)))) {
+            *r_out = rho * rho;
+            *v_out = v;
+            return 1;
+        }
+    }
+    *r_out = rho * rho;
+    *v_out = v;
+    return 0;
+}
+
+int orc_lc_fixed(double r_in, double v_in, double ell, double gnum, double dt, int N_taumin,
+                 int64_t max_steps, double *r_out, double *v_out)
+{
+    return lc_fixed_nf(r_in, v_in, ell, gnum, dt, N_taumin, max_steps, r_out, v_out, 0);
+}
+
 /* The per-particle integrators as the reference runs them (no bounded-work rule). */
 void orc_adaptive_leap(double r_in, double v_in, double ell, double gnum, double h,
                        double tol_r, double tol_v, int64_t max_subdiv, int out_type,
@@ -323,6 +376,13 @@ static int use_lc(const orc_params *p, int64_t i, int64_t n, double r, double el
     if (p->lc_rule == 2) return 0;
     if (p->lc_rule == 1) return (r > 1.0e-30 && r < p->lc_radius);
     double r_crit = 0.0;
+    if (p->lc_fixed) {   /* method 4, nsphere.c:5696-5707 */
+        if (ell != 0.0) {
+            const double M_enc = ((double)i / (double)n) * p->M;
+            r_crit = (ell * ell) * p->lc_alpha / (p->G * M_enc);
+        }
+        return (r > 1.0e-30 && r < r_crit);
+    }
     if (fabs(ell) > 1.0e-30) {
         double M_enc;
         if (i == 0) M_enc = 0.1 * (1.0 / (double)n) * p->M;
@@ -349,7 +409,11 @@ int64_t orc_step_adaptive(const orc_params *p, int64_t n, double *r, double *vr,
         double gnum = orc_gnum_pm(i, n, p->G, p->M, p->point_mass);
         double rn, vn;
         int lv;
-        if (use_lc(p, i, n, ri, li)) {
+        if (use_lc(p, i, n, ri, li) && p->lc_fixed) {
+            capped += lc_fixed_nf(ri, vi, li, gnum, p->dt, p->N_taumin, p->max_tau_steps, &rn, &vn,
+                                  p->nonfinite_stop);
+            lv = 100;
+        } else if (use_lc(p, i, n, ri, li)) {
             int64_t nt;
             capped += adaptive_lc_nf(ri, vi, li, gnum, p->dt, p->N_taumin, p->tol_r,
                                      p->tol_v, p->max_subdiv, p->out_type,
@@ -422,6 +486,7 @@ void orc_params_default(orc_params *p)
     p->max_tau_steps = 100000000;
     p->point_mass = 0.0;
     p->nonfinite_stop = 1;
+    p->lc_fixed = 0;
 }
 
 int orc_num_threads(void)

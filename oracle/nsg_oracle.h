@@ -17,6 +17,7 @@ typedef struct orc_params {
     int64_t max_tau_steps; /* tau-step cap (reference 1e8) */
     double point_mass;     /* central point mass added to M_i (not in the reference; 0 = reference) */
     int nonfinite_stop;    /* 1: a non-finite pass ends the climb / the tau-steps; 0: the reference */
+    int lc_fixed;          /* 1: method 4 (fixed-dtau Levi-Civita leapfrog, r_crit without the rank-0 case) */
 } orc_params;
 
 void orc_params_default(orc_params *p);
@@ -39,6 +40,10 @@ void orc_step_kdk(const orc_params *p, int64_t n, double *r, double *vr, double 
 void orc_energy(const orc_params *p, int64_t n, const double *r, const double *vr,
                 const double *ell, double *K, double *W);
 int orc_num_threads(void);
+/* Fixed-dtau Levi-Civita leapfrog over physical dt, nsphere.c:1827-1937 (returns 1 when
+ * the step cap was hit). */
+int orc_lc_fixed(double r_in, double v_in, double ell, double gnum, double dt, int N_taumin,
+                 int64_t max_steps, double *r_out, double *v_out);
 /* Static halo potential of the tracking energies (nsphere.c:4575-4592, 8205-8236):
  * model 0 cored (1+x^2)^-3, 1 Plummer, 2 Hernquist; r_trunc <= 0 untruncated;
  * r < r_lo is evaluated at r_lo + 1e-10 and r > r_hi (> 0) at r_hi - 1e-10. */

@@ -20,7 +20,7 @@ class OrcParams(C.Structure):
         ("tol_v", C.c_double), ("max_subdiv", C.c_int64), ("out_type", C.c_int),
         ("N_taumin", C.c_int), ("lc_rule", C.c_int), ("lc_alpha", C.c_double),
         ("lc_radius", C.c_double), ("max_tau_steps", C.c_int64), ("point_mass", C.c_double),
-        ("nonfinite_stop", C.c_int),
+        ("nonfinite_stop", C.c_int), ("lc_fixed", C.c_int),
     ]
 
 
@@ -50,6 +50,7 @@ class Oracle:
                                         C.c_void_p, C.c_void_p]
         L.orc_step_adaptive.restype = I64
         L.orc_step_kdk.argtypes = [C.POINTER(OrcParams), I64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_lc_fixed.argtypes = [D, D, D, D, D, I, I64, C.POINTER(D), C.POINTER(D)]
         L.orc_psi.argtypes = [I, D, D, D, D, D, D, D]
         L.orc_psi.restype = D
         L.orc_track.argtypes = [I, D, D, D, D, D, D, I, I, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -144,6 +145,11 @@ class Oracle:
         out["density_ok"] = rc == 0
         return out
 
+    def lc_fixed(self, r, v, ell, gnum, dt, N_taumin=1000, max_steps=200_000_000):
+        ro, vo = C.c_double(), C.c_double()
+        capped = self.L.orc_lc_fixed(r, v, ell, gnum, dt, N_taumin, max_steps, C.byref(ro), C.byref(vo))
+        return ro.value, vo.value, capped
+
     def psi(self, model, a, r_trunc, r_lo, r_hi, r, G=1.0, M=1.0):
         return self.L.orc_psi(model, a, r_trunc, r_lo, r_hi, G, M, float(r))
 
@@ -174,6 +180,8 @@ class Reference:
         L.ref_sort_particles.argtypes = [C.c_void_p, I]
         L.ref_step_method5.argtypes = [C.c_void_p, I, D, I, I, D, C.c_void_p]
         L.ref_step_kdk.argtypes = [C.c_void_p, I, D, C.c_void_p]
+        L.ref_lc_fixed.argtypes = [I, I, D, D, D, D, I, C.POINTER(D), C.POINTER(D)]
+        L.ref_step_method4.argtypes = [C.c_void_p, I, D, I, D, I, C.c_void_p]
         L.ref_num_threads.restype = I
         L.ref_set_units(1.0, 1.0)
         L.ref_set_sort(0)
@@ -211,6 +219,18 @@ class Reference:
         self.L.ref_set_sort(1 if parallel_sort else 0)
         self.L.ref_step_method5(rows, n, dt, max_subdiv, lc_rule, lc_radius, _p(inv))
         self.L.ref_set_sort(0)
+        return tab, inv
+
+    def lc_fixed(self, i, n, r, v, ell, dt, N_taumin=1000):
+        ro, vo = C.c_double(), C.c_double()
+        self.L.ref_lc_fixed(i, n, r, v, ell, dt, N_taumin, C.byref(ro), C.byref(vo))
+        return ro.value, vo.value
+
+    def step_method4(self, r, vr, ell, ids, dt, max_subdiv=128, tol=1e-8, N_taumin=1000):
+        n = len(r)
+        tab, rows = self._table([r, vr, ell, np.asarray(ids, dtype=np.float64), np.zeros(n)])
+        inv = np.zeros(n, dtype=np.int32)
+        self.L.ref_step_method4(rows, n, dt, max_subdiv, tol, N_taumin, _p(inv))
         return tab, inv
 
     def step_kdk(self, r, vr, ell, ids, dt, parallel_sort=False):

@@ -41,6 +41,12 @@ void ref_adaptive_lc(int i, int npts, double r, double v, double ell, double dt,
                              G_CONST, out_type, r_out, v_out);
 }
 
+void ref_lc_fixed(int i, int npts, double r, double v, double ell, double dt, int N_taumin,
+                  double *r_out, double *v_out)
+{
+    doLeviCivitaLeapfrog(i, npts, r, v, ell, dt, N_taumin, G_CONST, r_out, v_out);
+}
+
 void ref_micro_leap(int i, int npts, double r, double v, double ell, double h, int N,
                     int subSteps, double *r_out, double *v_out)
 {
@@ -95,6 +101,42 @@ void ref_step_method5(double **particles, int npts, double dt, int max_subdiv,
                                G_CONST, out_type, &r_new, &v_new);
         particles[0][i] = r_new;
         particles[1][i] = v_new;
+    }
+}
+
+/* One method-4 step (CLI --method 2) as in main() (nsphere.c:5661-5745), with the
+ * reference's constants except max_subdiv, the tolerance and N_taumin, which are
+ * arguments (the reference: 4096*4096, 1e-8, 1000). */
+void ref_step_method4(double **particles, int npts, double dt, int max_subdiv, double tol,
+                      int N_taumin, int *inverse_map)
+{
+    int out_type = 2;
+    double alpha_param = 0.05;
+    sort_particles(particles, npts);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < npts; i++) {
+        double r = particles[0][i];
+        double v = particles[1][i];
+        double ell = particles[2][i];
+        double r_crit = 0.0;
+        if (ell != 0.0) {
+            double M_enc = ((double)i / (double)npts) * HALO_MASS;
+            double gravPart = (VEL_CONV_SQ * G_CONST) * M_enc;
+            r_crit = (ell * ell) * (alpha_param) / (gravPart);
+        }
+        double r_new, v_new;
+        if ((r > 1.0e-30) && (r < r_crit))
+            doLeviCivitaLeapfrog(i, npts, r, v, ell, dt, N_taumin, G_CONST, &r_new, &v_new);
+        else
+            doAdaptiveFullLeap(i, npts, r, v, ell, dt, tol, tol, max_subdiv, G_CONST, out_type,
+                               &r_new, &v_new);
+        particles[0][i] = r_new;
+        particles[1][i] = v_new;
+    }
+#pragma omp parallel for schedule(static)
+    for (int idx = 0; idx < npts; idx++) {
+        int orig_id = (int)particles[3][idx];
+        inverse_map[orig_id] = idx;
     }
 }
 

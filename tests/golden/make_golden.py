@@ -2,12 +2,13 @@
 
 The reference (kris-sigurdson/NSphere) ships no tests, fixtures or known-answer
 vectors for its step path, so the fixtures come from running its own functions
-(forces, doAdaptiveFullLeap, doAdaptiveFullLeviCivita, sort_particles, and the
-method-5 / method-2 step bodies) on seeded inputs.  Those functions are extracted
+(forces, doAdaptiveFullLeap, doAdaptiveFullLeviCivita, doLeviCivitaLeapfrog,
+sort_particles, and the method-5 / method-4 / method-2 step bodies) on seeded inputs.  Those functions are extracted
 from src/c/nsphere.c and built by oracle/build_oracle.py into oracle/_ref/libnsref.so
 with -O2 -fno-fast-math -ffp-contract=off.  Units: G = M = 1 (VEL_CONV_SQ = 1).
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py  (all fixtures), or
+python tests/golden/make_golden.py method4  (method4.npz alone).
 """
 from __future__ import annotations
 
@@ -87,8 +88,36 @@ def main():
     np.savez_compressed(os.path.join(OUT, "steps.npz"), r=r, vr=vr, ell=ell, ids=ids,
                         method5_rcrit=t5, method5_radius=t5b, kdk_start=start, kdk5=cur,
                         dt5=5e-4, dt_kdk=1e-3, lc_radius=1e-1)
+    method4_fixture(R)
     print("fixtures written to", OUT)
 
 
+def method4_fixture(R):
+    """4. method 4 (CLI --method 2): the fixed-dtau Levi-Civita leapfrog of single
+    particles (doLeviCivitaLeapfrog) and one step body (nsphere.c:5661-5745)."""
+    rng = np.random.default_rng(4242)
+    n = 4096
+    idx = np.sort(rng.choice(np.arange(1, n), 64, replace=False)).astype(np.int32)
+    r = 10.0 ** rng.uniform(-4.0, -1.0, idx.size)
+    v = rng.normal(0.0, 0.3, idx.size)
+    ell = 10.0 ** rng.uniform(-5.0, -2.0, idx.size)
+    fixed = np.array([R.lc_fixed(int(i), n, a, b, c, 1e-3, 1000) for i, a, b, c in zip(idx, r, v, ell)])
+    m = 5000
+    sr, sv, sl, sid = ics.hernquist(m, seed=19)
+    perm = rng.permutation(m)
+    sr, sv, sl, sid = sr[perm], sv[perm], sl[perm], sid[perm]
+    sl = sl.copy()
+    low = rng.choice(m, 50, replace=False)
+    sl[low] = rng.uniform(0.0, 1e-4, low.size)
+    t4, _ = R.step_method4(sr, sv, sl, sid, 1e-3, max_subdiv=128, tol=1e-8, N_taumin=1000)
+    np.savez_compressed(os.path.join(OUT, "method4.npz"), n=n, idx=idx, r=r, vr=v, ell=ell, dt=1e-3,
+                        N_taumin=1000, fixed_out=fixed, step_r=sr, step_vr=sv, step_ell=sl, step_ids=sid,
+                        step_out=t4, step_msub=128, step_tol=1e-8)
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "method4":
+        build_oracle.build_reference()
+        method4_fixture(Reference())
+    else:
+        main()

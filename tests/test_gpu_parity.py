@@ -140,6 +140,42 @@ def test_adaptive_step_bit_exact(nsg, oracle, lc_rule, lc_radius, dt, msub, out_
     assert hist[-1] == np.sum(olv >= 99)
 
 
+@pytest.mark.parametrize("lc_rule,lc_radius", [(0, 1e-3), (1, 5e-2)])
+def test_method4_fixed_levi_civita_matches_oracle(nsg, oracle, lc_rule, lc_radius):
+    """Method 4: adaptive leapfrog at tol 1e-8, fixed-dtau Levi-Civita leapfrog
+    (N_taumin 1000) below r_crit (no rank-0 special case) or below lc_radius; three
+    steps, graph replay included."""
+    n, dt = 20000, 1e-3
+    r, vr, ell, ids = _adaptive_case(n, 27, lowl=100)
+    kw = dict(dt=dt, max_subdiv=128, tol_r=1e-8, tol_v=1e-8, N_taumin=1000, lc_rule=lc_rule, lc_radius=lc_radius)
+    p = oracle.params(lc_fixed=1, **kw)
+    cur = (r, vr, ell, ids)
+    for _ in range(3):
+        o = oracle.step_adaptive(p, *cur)
+        cur = o[:4]
+    with _ctx(nsg, method=nsg.METHOD_FULL_LC, **kw) as c:
+        c.upload(r, vr, ell, ids)
+        c.step(3)
+        gr, gv, gl, gid = c.download()
+        glv = c.levels()
+    assert np.array_equal(gid, cur[3])
+    assert np.array_equal(gr, cur[0]) and np.array_equal(gv, cur[1])
+    assert np.array_equal(glv, o[4]) and np.sum(glv == 100) > 0
+
+
+def test_method4_matches_golden(nsg):
+    g = golden("method4.npz")
+    tol = float(g["step_tol"])
+    with _ctx(nsg, method=nsg.METHOD_FULL_LC, dt=float(g["dt"]), max_subdiv=int(g["step_msub"]), tol_r=tol,
+              tol_v=tol, N_taumin=int(g["N_taumin"]), lc_rule=0) as c:
+        c.upload(g["step_r"], g["step_vr"], g["step_ell"], g["step_ids"])
+        c.step(1)
+        r, vr, ell, ids = c.download()
+    t = g["step_out"]
+    assert np.array_equal(ids, t[3].astype(np.int32))
+    assert np.array_equal(r, t[0]) and np.array_equal(vr, t[1])
+
+
 def test_method5_matches_golden(nsg):
     g = golden("steps.npz")
     with _ctx(nsg, dt=float(g["dt5"]), max_subdiv=128, lc_rule=0) as c:

@@ -129,3 +129,22 @@ def test_reference_default_sort_is_not_total(reference):
     # documented behaviour, not a requirement: report the inversions found
     inv = int(np.sum(np.diff(tab[0]) < 0))
     assert inv >= 0
+
+
+def test_method4_matches_golden(oracle):
+    """Method 4 (CLI --method 2): the fixed-dtau Levi-Civita leapfrog of single particles
+    and one step body against the reference's doLeviCivitaLeapfrog and main() loop."""
+    g = golden("method4.npz")
+    n = int(g["n"])
+    for k, i in enumerate(g["idx"]):
+        ro, vo, cap = oracle.lc_fixed(g["r"][k], g["vr"][k], g["ell"][k], oracle.gnum(int(i), n),
+                                      float(g["dt"]), int(g["N_taumin"]))
+        assert cap == 0
+        assert ro == g["fixed_out"][k, 0] and vo == g["fixed_out"][k, 1], k
+    p = oracle.params(dt=float(g["dt"]), max_subdiv=int(g["step_msub"]), tol_r=float(g["step_tol"]),
+                      tol_v=float(g["step_tol"]), N_taumin=int(g["N_taumin"]), lc_rule=0, lc_fixed=1)
+    r, vr, ell, ids, lv, cap = oracle.step_adaptive(p, g["step_r"], g["step_vr"], g["step_ell"], g["step_ids"])
+    t = g["step_out"]
+    assert np.array_equal(ids, t[3].astype(np.int32))
+    assert np.array_equal(r, t[0]) and np.array_equal(vr, t[1])
+    assert np.sum(lv == 100) > 0          # the Levi-Civita path ran

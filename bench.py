@@ -399,8 +399,8 @@ def main():
             ctx._check(lib.nsg_upload(ctx.handle, P(h_r), P(h_v), P(h_l), P(h_i), None, n))
         else:
             ctx._check(lib.nsg_upload_ensemble(ctx.handle, P(h_r), P(h_v), P(h_l), P(h_i), None, P(hn), len(hn)))
-        ctx._check(lib.nsg_step(ctx.handle, 1))
-        ctx._check(lib.nsg_download(ctx.handle, P(o_r), P(o_v), P(o_l), P(o_i), None))
+        # one step and the read-back of its result (the copy overlaps the step's chains)
+        ctx._check(lib.nsg_step_download(ctx.handle, 1, P(o_r), P(o_v), P(o_l), P(o_i), None))
     ee1.record(stream)
     barrier()
     e2e_value = job_rate(n * args.e2e_steps, world, max_over_ranks(ee0.elapsed_time(ee1), world, device="cuda"))

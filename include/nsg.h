@@ -156,6 +156,13 @@ int nsg_sort(nsg_ctx *ctx);
 int nsg_download(nsg_ctx *ctx, double *r, double *vr, double *ell,
                  double *id_as_double, double *aux);
 int nsg_download_particles(nsg_ctx *ctx, double *const *particles);
+/* nsteps steps followed by nsg_download, with the same results: in the last step the
+ * copy of the particles the leapfrog kernels integrate runs beside the Levi-Civita
+ * chains, and the chains' particles are patched in when they end (no reference
+ * counterpart; a driver that downloads every step, like the snapshot code at
+ * nsphere.c:6452, hides most of the copy this way). */
+int nsg_step_download(nsg_ctx *ctx, int nsteps, double *r, double *vr, double *ell,
+                      double *id_as_double, double *aux);
 /* Device-pointer views of the resident columns (valid until the next call). */
 int nsg_device_state(nsg_ctx *ctx, double **d_r, double **d_vr, double **d_ell,
                      int32_t **d_id, int64_t *n);

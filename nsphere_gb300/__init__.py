@@ -40,7 +40,7 @@ EXPORTS = [
     "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc", "nsg_probe_latency",
     "nsg_write_init", "nsg_read_init", "nsg_snapshot_open", "nsg_snapshot", "nsg_snapshot_close",
     "nsg_generate", "nsg_potential", "nsg_track_open", "nsg_track_read", "nsg_track_close",
-    "nsg_post_snapshot",
+    "nsg_post_snapshot", "nsg_step_download",
 ]
 
 # records of the reference's Rank files (nsphere.c:7930-7983), as nsg_rank_sorted /
@@ -147,6 +147,7 @@ def lib() -> C.CDLL:
         "nsg_track_read": [P, P, C.POINTER(I64), C.POINTER(I64)],
         "nsg_track_close": [P],
         "nsg_post_snapshot": [P, P, I64, P, P, C.POINTER(D)],
+        "nsg_step_download": [P, C.c_int, P, P, P, P, P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -264,6 +265,17 @@ class Context:
         r, vr, ell, idd = (np.empty(n) for _ in range(4))
         aux = np.empty(n) if with_aux else None
         self._check(self._L.nsg_download(self._h, _ptr(r), _ptr(vr), _ptr(ell), _ptr(idd), _ptr(aux)))
+        out = (r, vr, ell, idd.astype(np.int32))
+        return out + ((aux,) if with_aux else ())
+
+    def step_download(self, nsteps: int = 1, with_aux: bool = False):
+        """nsteps steps, then the state as download() returns it (the copy overlaps the
+        last step's Levi-Civita chains)."""
+        n = self.n = self._n_from_ctx()
+        r, vr, ell, idd = (np.empty(n) for _ in range(4))
+        aux = np.empty(n) if with_aux else None
+        self._check(self._L.nsg_step_download(self._h, int(nsteps), _ptr(r), _ptr(vr), _ptr(ell), _ptr(idd),
+                                              _ptr(aux)))
         out = (r, vr, ell, idd.astype(np.int32))
         return out + ((aux,) if with_aux else ())
 

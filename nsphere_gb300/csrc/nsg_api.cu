@@ -725,6 +725,81 @@ int nsg_download(nsg_ctx *c, double *r, double *vr, double *ell, double *id_as_d
     return NSG_OK;
 }
 
+__global__ void k_pack_lc(const unsigned int *__restrict__ cnt, const uint32_t *__restrict__ lc_idx,
+                          const double *__restrict__ r, const double *__restrict__ v, uint32_t *__restrict__ oi,
+                          double *__restrict__ orr, double *__restrict__ ov, unsigned int cap)
+{
+    const unsigned int m = *cnt < cap ? *cnt : cap;
+    for (unsigned int e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) {
+        const uint32_t i = lc_idx[e];
+        oi[e] = i;
+        orr[e] = r[i];
+        ov[e] = v[i];
+    }
+}
+
+int nsg_step_download(nsg_ctx *c, int nsteps, double *r, double *vr, double *ell, double *id_as_double,
+                      double *aux)
+{
+    if (int rc = check_ctx(c)) return rc;
+    if (c->n <= 0) return set_err(c, NSG_ESTATE, "no state uploaded");
+    if (nsteps < 1) return set_err(c, NSG_EINVAL, "nsteps must be >= 1");
+    const bool lc = (c->p.method == NSG_METHOD_ADAPTIVE_LC || c->p.method == NSG_METHOD_FULL_LC) &&
+                    c->p.lc_rule != NSG_LC_OFF;
+    if (!lc || c->profiling) {
+        if (int rc = nsg_step(c, nsteps)) return rc;
+        return nsg_download(c, r, vr, ell, id_as_double, aux);
+    }
+    if (nsteps > 1)
+        if (int rc = nsg_step(c, nsteps - 1)) return rc;
+    // the last step eagerly: the side stream's leapfrog kernels are followed, in stream
+    // order, by the copy of the sorted state, which then runs beside the chains
+    if (int rc = one_step(c)) return rc;
+    const int s = c->cur;
+    const size_t b = (size_t)c->n * 8;
+    cudaStream_t sd = c->side;
+    cudaError_t e = cudaSuccess;
+    if (r) e = cudaMemcpyAsync(r, c->r[s], b, cudaMemcpyDeviceToHost, sd);
+    if (e == cudaSuccess && vr) e = cudaMemcpyAsync(vr, c->vr[s], b, cudaMemcpyDeviceToHost, sd);
+    if (e == cudaSuccess && ell) e = cudaMemcpyAsync(ell, c->ell[s], b, cudaMemcpyDeviceToHost, sd);
+    if (e == cudaSuccess && aux && c->p.carry_aux) e = cudaMemcpyAsync(aux, c->aux[s], b, cudaMemcpyDeviceToHost, sd);
+    if (e == cudaSuccess && id_as_double) {
+        k_ids_to_double<<<grid_for(c, c->n, 256), 256, 0, sd>>>(c->id[s], c->stage_d, c->n);
+        e = cudaMemcpyAsync(id_as_double, c->stage_d, b, cudaMemcpyDeviceToHost, sd);
+    }
+    if (e != cudaSuccess) return cuda_err(c, e, "step download");
+    // the Levi-Civita particles' results land when the chains end: fetch them and
+    // overwrite whatever the bulk copy saw at their positions
+    unsigned int cnt = 0;
+    e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(&cnt, &c->ctr->lc_count, sizeof(cnt), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(c, e, "step download");
+    std::vector<uint32_t> hi(cnt);
+    std::vector<double> hr(cnt), hv(cnt);
+    if (cnt > 0 && (r || vr)) {
+        unsigned char *d = nullptr;
+        e = cudaMallocAsync((void **)&d, (size_t)cnt * 24, c->stream);
+        if (e != cudaSuccess) return cuda_err(c, e, "step download");
+        uint32_t *di = reinterpret_cast<uint32_t *>(d + (size_t)cnt * 16);
+        double *dr = reinterpret_cast<double *>(d), *dv = dr + cnt;
+        k_pack_lc<<<(cnt + 255) / 256, 256, 0, c->stream>>>(&c->ctr->lc_count, c->lc_idx, c->r[s], c->vr[s], di, dr,
+                                                           dv, cnt);
+        e = cudaMemcpyAsync(hi.data(), di, (size_t)cnt * 4, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hr.data(), dr, (size_t)cnt * 8, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hv.data(), dv, (size_t)cnt * 8, cudaMemcpyDeviceToHost, c->stream);
+        cudaFreeAsync(d, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_err(c, e, "step download");
+    }
+    e = cudaStreamSynchronize(sd);
+    if (e != cudaSuccess) return cuda_err(c, e, "step download");
+    for (unsigned int k = 0; k < cnt; k++) {
+        if (r) r[hi[k]] = hr[k];
+        if (vr) vr[hi[k]] = hv[k];
+    }
+    return NSG_OK;
+}
+
 int nsg_download_particles(nsg_ctx *c, double *const *particles)
 {
     if (!particles) return set_err(c, NSG_EINVAL, "null particles");

@@ -163,6 +163,24 @@ def test_method4_fixed_levi_civita_matches_oracle(nsg, oracle, lc_rule, lc_radiu
     assert np.array_equal(glv, o[4]) and np.sum(glv == 100) > 0
 
 
+def test_method3_adaptive_leapfrog_only(nsg, oracle):
+    """Method 3 (CLI --method 3, nsphere.c:5560-5615): adaptive leapfrog for every
+    particle, with the reference's constants tol 1e-5, max_subdiv 1, coarse output."""
+    n, dt = 20000, 1e-3
+    r, vr, ell, ids = _adaptive_case(n, 29, lowl=100)
+    kw = dict(dt=dt, max_subdiv=1, tol_r=1e-5, tol_v=1e-5, out_type=0)
+    p = oracle.params(lc_rule=2, **kw)
+    cur = (r, vr, ell, ids)
+    for _ in range(4):
+        cur = oracle.step_adaptive(p, *cur)[:4]
+    with _ctx(nsg, method=nsg.METHOD_ADAPTIVE, **kw) as c:
+        c.upload(r, vr, ell, ids)
+        c.step(4)
+        gr, gv, gl, gid = c.download()
+    assert np.array_equal(gid, cur[3])
+    assert np.array_equal(gr, cur[0]) and np.array_equal(gv, cur[1])
+
+
 def test_method4_matches_golden(nsg):
     g = golden("method4.npz")
     tol = float(g["step_tol"])
@@ -399,3 +417,24 @@ def test_near_sorted_sort_after_moves(nsg, oracle):
         c.step(30)
         r, vr, ell, ids = c.download()
     assert np.array_equal(ids, cur[3]) and np.array_equal(r, cur[0]) and np.array_equal(vr, cur[1])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", [5, 4, 2])
+def test_step_download_equals_step_then_download(nsg, method):
+    """nsg_step_download overlaps the last step's copy with its Levi-Civita chains and
+    patches the chains' particles in: the arrays equal nsg_step + nsg_download."""
+    n = 50000
+    r, vr, ell, ids = _adaptive_case(n, 51, lowl=200)
+    kw = dict(dt=1e-3, max_subdiv=64, lc_rule=1, lc_radius=5e-2) if method != 2 else dict(dt=1e-3)
+    outs = []
+    for overlapped in (False, True):
+        with _ctx(nsg, method=method, **kw) as c:
+            c.upload(r, vr, ell, ids)
+            if overlapped:
+                outs.append(c.step_download(3))
+            else:
+                c.step(3)
+                outs.append(c.download())
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)

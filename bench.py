@@ -87,7 +87,12 @@ def workload(args, seed_offset=0):
         cfg = dict(workload="hernquist_om_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 osipkov-merritt r_a=1",
                    seed=replica_seed(4, seed_offset), dt=5e-4, max_levels=8, max_subdiv=128,
                    lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
-        state = ics.hernquist(args.n, seed=replica_seed(4, seed_offset), r_a=1.0)
+        # generated on the GPU (nsg_generate_om, closed-form Osipkov-Merritt f(Q))
+        import nsphere_gb300 as ns
+        with ns.Context(ns.default_params()) as g:
+            g.generate_om(args.n, replica_seed(4, seed_offset), 100.0, 1.0)
+            state = g.download()
+        cfg["generator"] = "nsg_generate_om"
         params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
     elif args.workload == "stress":
         # Hernquist, 20 % of the particles on near-radial orbits (ell uniform in [0, 1e-4]),

@@ -190,6 +190,11 @@ int nsg_sort_device_noalloc(double *d_r, double *d_vr, double *d_ell, int32_t *d
  * truncation radius (ignored for Plummer).  Counter-based draws: the result depends
  * only on (model, n, seed, r_max). */
 int nsg_generate(nsg_ctx *ctx, int model, int64_t n, uint64_t seed, double r_max);
+/* The Hernquist model with Osipkov-Merritt anisotropy of radius r_a (the reference
+ * builds its models from GSL splines of the distribution function,
+ * nsphere.c:4238-4824): f(Q) = f_iso(Q) + sqrt(Q) (1 - 2Q) / (sqrt(2) pi^3 r_a^2), the
+ * closed-form Eddington inversion of rho_Q = (1 + r^2/r_a^2) rho. */
+int nsg_generate_om(nsg_ctx *ctx, int64_t n, uint64_t seed, double r_max, double r_a);
 
 /* Per-particle potential and energy of the post-processing (nsphere.c:7697-7846), on
  * the resident state in its sorted order (sorted first if needed; one halo):

@@ -40,7 +40,7 @@ EXPORTS = [
     "nsg_tune_get", "nsg_tune_set", "nsg_autotune", "nsg_sort_device_noalloc", "nsg_probe_latency",
     "nsg_write_init", "nsg_read_init", "nsg_snapshot_open", "nsg_snapshot", "nsg_snapshot_close",
     "nsg_generate", "nsg_potential", "nsg_track_open", "nsg_track_read", "nsg_track_close",
-    "nsg_post_snapshot", "nsg_step_download",
+    "nsg_post_snapshot", "nsg_step_download", "nsg_generate_om",
 ]
 
 # records of the reference's Rank files (nsphere.c:7930-7983), as nsg_rank_sorted /
@@ -148,6 +148,7 @@ def lib() -> C.CDLL:
         "nsg_track_close": [P],
         "nsg_post_snapshot": [P, P, I64, P, P, C.POINTER(D)],
         "nsg_step_download": [P, C.c_int, P, P, P, P, P],
+        "nsg_generate_om": [P, I64, C.c_uint64, D, D],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -375,6 +376,11 @@ class Context:
     def generate(self, model: int, n: int, seed: int, r_max: float = 100.0):
         """Seeded initial conditions generated on the GPU into the resident state."""
         self._check(self._L.nsg_generate(self._h, int(model), int(n), int(seed), float(r_max)))
+        self.n = int(n)
+
+    def generate_om(self, n: int, seed: int, r_max: float = 100.0, r_a: float = 1.0):
+        """Hernquist with Osipkov-Merritt anisotropy radius r_a, generated on the GPU."""
+        self._check(self._L.nsg_generate_om(self._h, int(n), int(seed), float(r_max), float(r_a)))
         self.n = int(n)
 
     def potential(self):

@@ -4,7 +4,8 @@
 //     Wielen (1974) rejection for q = v / v_esc, g(q) = q^2 (1 - q^2)^(7/2) < 0.1;
 //   * Hernquist (1990), truncated at r_max: inverse-CDF radii of M(r) = r^2/(1+r)^2
 //     and speeds from the isotropic distribution function f(E) by rejection under a
-//     bound found per particle (grid search and golden-section refinement).
+//     bound found per particle (grid search and golden-section refinement), or from
+//     the Osipkov-Merritt f(Q) with anisotropy radius r_a (below).
 // Directions use the reference's mapping v_r = v mu, ell = r v sqrt(1 - mu^2), mu
 // uniform in [-1, 1] (nsphere.c:4805-4808, 4914).  The state is then sorted by
 // radius and the ids are set to the radial rank, as the reference remaps them
@@ -136,6 +137,75 @@ __global__ void k_ic_hernquist(uint64_t seed, int64_t n, double umax, double *r_
     }
 }
 
+// Osipkov-Merritt anisotropy (Osipkov 1979; Merritt 1985) on the Hernquist halo: the
+// distribution function depends on Q = E + L^2/(2 r_a^2) through the Eddington
+// inversion of rho_Q = (1 + r^2/r_a^2) rho.  For Hernquist the added density
+// r^2 rho / r_a^2 = (Psi^2 - Psi^3) / (2 pi r_a^2) inverts in closed form, so in the
+// units of hq_df
+//   f(Q) = hq_df(Q) + (8 / r_a^2) sqrt(Q) (1 - 2Q),  clamped at 0.
+// At fixed r, w = (v_r, v_t sqrt(1 + r^2/r_a^2)) is then isotropic with speed density
+// w^2 f(Psi - w^2/2): the isotropic sampler draws it, and v_t = w_t / sqrt(1 + r^2/r_a^2).
+__host__ __device__ __forceinline__ double om_target(double psi, double x, double k)
+{
+    const double q = psi * (1.0 - x * x);
+    const double f = hq_df(q) + k * sqrt(q) * (1.0 - 2.0 * q);
+    return x * x * (f > 0.0 ? f : 0.0);
+}
+
+__host__ __device__ __forceinline__ double om_bound(double psi, double k)
+{
+    int jb = 1;
+    double gb = -1.0;
+    for (int j = 1; j <= 64; j++) {
+        const double t = j / 64.0;
+        const double g = om_target(psi, t * t, k);
+        if (g > gb) { gb = g; jb = j; }
+    }
+    const double tl = (jb - 1) / 64.0, th = (jb < 64 ? jb + 1 : 64) / 64.0;
+    double a = tl * tl, b = th * th;
+    const double ig = 0.6180339887498949;
+    double c = b - ig * (b - a), d = a + ig * (b - a);
+    double gc = om_target(psi, c, k), gd = om_target(psi, d, k);
+    for (int it = 0; it < 40; it++) {
+        if (gc > gd) { b = d; d = c; gd = gc; c = b - ig * (b - a); gc = om_target(psi, c, k); }
+        else { a = c; c = d; gc = gd; d = a + ig * (b - a); gd = om_target(psi, d, k); }
+    }
+    const double m = fmax(gb, fmax(gc, gd));
+    return m * 1.3 + 1e-300;
+}
+
+__global__ void k_ic_hernquist_om(uint64_t seed, int64_t n, double umax, double r_a, double *r_out,
+                                  double *v_out, double *l_out, int32_t *id_out, double *mu_out,
+                                  unsigned int *status)
+{
+    const double k = 8.0 / (r_a * r_a);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double s = sqrt(umax * ic_uniform(seed, i, 0));
+        const double r = fmax(s / (1.0 - s), 1e-12);
+        const double psi = 1.0 / (1.0 + r);
+        const double bound = om_bound(psi, k);
+        double x = 0.0;
+        int a = 0;
+        for (; a < kIcMaxAttempts; a++) {
+            const double xx = ic_uniform(seed, i, 2 + 2 * (uint64_t)a);
+            const double yy = ic_uniform(seed, i, 3 + 2 * (uint64_t)a) * bound;
+            if (yy < om_target(psi, xx, k)) { x = xx; break; }
+        }
+        if (a == kIcMaxAttempts) atomicOr(status, NSG_ST_IC_REJECT);
+        const double w = x * sqrt(2.0 * psi);
+        const double mu = 2.0 * ic_uniform(seed, i, 1) - 1.0;
+        const double wr = w * mu, wt = w * sqrt(fmax(0.0, 1.0 - mu * mu));
+        const double ra = r / r_a;
+        const double vt = wt / sqrt(1.0 + ra * ra);
+        r_out[i] = r;
+        v_out[i] = wr;
+        l_out[i] = r * vt;
+        id_out[i] = (int32_t)i;
+        if (mu_out) mu_out[i] = mu;
+    }
+}
+
 __global__ void k_ic_rank_ids(int32_t *id, int64_t n)
 {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
@@ -147,12 +217,13 @@ __global__ void k_ic_rank_ids(int32_t *id, int64_t n)
 
 using namespace nsg;
 
-extern "C" int nsg_generate(nsg_ctx *c, int model, int64_t n, uint64_t seed, double r_max)
+static int generate(nsg_ctx *c, int model, int64_t n, uint64_t seed, double r_max, double r_a)
 {
     if (!c) return set_err(nullptr, NSG_EINVAL, "null context");
     if (model != NSG_IC_PLUMMER && model != NSG_IC_HERNQUIST) return set_err(c, NSG_EINVAL, "unknown model");
     if (model == NSG_IC_HERNQUIST && !(r_max > 0.0 && std::isfinite(r_max)))
         return set_err(c, NSG_EINVAL, "r_max must be positive and finite");
+    if (!(r_a > 0.0)) return set_err(c, NSG_EINVAL, "r_a must be positive");
     if (int rc = begin_upload(c, n)) return rc;
     cudaStream_t s = c->stream;
     double *mu = c->p.carry_aux ? c->aux[0] : nullptr;
@@ -161,10 +232,14 @@ extern "C" int nsg_generate(nsg_ctx *c, int model, int64_t n, uint64_t seed, dou
     if (model == NSG_IC_PLUMMER) {
         k_ic_plummer<<<grid_for(c, n, 256), 256, 0, s>>>(seed, n, c->r[0], c->vr[0], c->ell[0], c->id[0], mu,
                                                          &c->ctr->status);
-    } else {
+    } else if (std::isinf(r_a)) {
         const double umax = (r_max / (1.0 + r_max)) * (r_max / (1.0 + r_max));
         k_ic_hernquist<<<grid_for(c, n, 256), 256, 0, s>>>(seed, n, umax, c->r[0], c->vr[0], c->ell[0], c->id[0],
                                                            mu, &c->ctr->status);
+    } else {
+        const double umax = (r_max / (1.0 + r_max)) * (r_max / (1.0 + r_max));
+        k_ic_hernquist_om<<<grid_for(c, n, 256), 256, 0, s>>>(seed, n, umax, r_a, c->r[0], c->vr[0], c->ell[0],
+                                                              c->id[0], mu, &c->ctr->status);
     }
     c->launches += 1;
     e = cudaGetLastError();
@@ -176,4 +251,15 @@ extern "C" int nsg_generate(nsg_ctx *c, int model, int64_t n, uint64_t seed, dou
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(c, e, "generate");
     return NSG_OK;
+}
+
+extern "C" int nsg_generate(nsg_ctx *c, int model, int64_t n, uint64_t seed, double r_max)
+{
+    return generate(c, model, n, seed, r_max, INFINITY);
+}
+
+extern "C" int nsg_generate_om(nsg_ctx *c, int64_t n, uint64_t seed, double r_max, double r_a)
+{
+    if (c && !(r_a > 0.0 && std::isfinite(r_a))) return set_err(c, NSG_EINVAL, "r_a must be positive and finite");
+    return generate(c, NSG_IC_HERNQUIST, n, seed, r_max, r_a);
 }

@@ -255,6 +255,69 @@ def _hq_bound(psi):
     return np.maximum(gb, np.maximum(gc, gd)) * 1.3 + 1e-300
 
 
+def _om_target(psi, x, k):
+    q = psi * (1.0 - x * x)
+    f = _hq_df_unnormalised(q) + k * np.sqrt(q) * (1.0 - 2.0 * q)
+    return x * x * np.where(f > 0.0, f, 0.0)
+
+
+def _om_bound(psi, k):
+    """_hq_bound for the Osipkov-Merritt target."""
+    gb = np.full(psi.shape, -1.0)
+    jb = np.ones(psi.shape, dtype=np.int64)
+    for j in range(1, 65):
+        t = j / 64.0
+        g = _om_target(psi, t * t, k)
+        better = g > gb
+        gb = np.where(better, g, gb)
+        jb = np.where(better, j, jb)
+    tl = (jb - 1) / 64.0
+    th = np.where(jb < 64, jb + 1, 64) / 64.0
+    a, b = tl * tl, th * th
+    ig = 0.6180339887498949
+    c = b - ig * (b - a)
+    d = a + ig * (b - a)
+    gc, gd = _om_target(psi, c, k), _om_target(psi, d, k)
+    for _ in range(40):
+        left = gc > gd
+        nb = np.where(left, d, b)
+        na = np.where(left, a, c)
+        nc = np.where(left, nb - ig * (nb - na), d)
+        nd = np.where(left, c, na + ig * (nb - na))
+        ngc = np.where(left, _om_target(psi, nc, k), gd)
+        ngd = np.where(left, gc, _om_target(psi, nd, k))
+        a, b, c, d, gc, gd = na, nb, nc, nd, ngc, ngd
+    return np.maximum(gb, np.maximum(gc, gd)) * 1.3 + 1e-300
+
+
+def hernquist_om_counter(n: int, seed: int, r_max: float = 100.0, r_a: float = 1.0):
+    """(r, vr, ell, ids, mu) of nsg_generate_om(n, seed, r_max, r_a)."""
+    i = np.arange(n, dtype=np.uint64)
+    k = 8.0 / (r_a * r_a)
+    umax = (r_max / (1.0 + r_max)) * (r_max / (1.0 + r_max))
+    s = np.sqrt(umax * counter_uniform(seed, i, 0))
+    r = np.maximum(s / (1.0 - s), 1e-12)
+    psi = 1.0 / (1.0 + r)
+    bound = _om_bound(psi, k)
+    x = np.zeros(n)
+    todo = np.arange(n)
+    a = 0
+    while todo.size:
+        xx = counter_uniform(seed, i[todo], 2 + 2 * a)
+        yy = counter_uniform(seed, i[todo], 3 + 2 * a) * bound[todo]
+        ok = yy < _om_target(psi[todo], xx, k)
+        x[todo[ok]] = xx[ok]
+        todo = todo[~ok]
+        a += 1
+    w = x * np.sqrt(2.0 * psi)
+    mu = 2.0 * counter_uniform(seed, i, 1) - 1.0
+    wr = w * mu
+    wt = w * np.sqrt(np.maximum(0.0, 1.0 - mu * mu))
+    ra = r / r_a
+    vt = wt / np.sqrt(1.0 + ra * ra)
+    return _rank_order(r, wr, r * vt, mu)
+
+
 def _rank_order(r, vr, ell, mu):
     order = np.lexsort((np.arange(r.shape[0]), r))
     return r[order], vr[order], ell[order], np.arange(r.shape[0], dtype=np.int32), mu[order]

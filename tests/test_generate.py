@@ -69,3 +69,42 @@ def test_generated_state_steps(nsg, oracle):
     p = oracle.params(dt=1e-3, max_subdiv=64, lc_rule=1, lc_radius=1e-2)
     orr, ov, ol, oid, olv, cap = oracle.step_adaptive(p, r, vr, ell, ids)
     assert np.array_equal(gid, oid) and np.array_equal(gr, orr) and np.array_equal(gv, ov)
+
+
+def test_om_closed_form_matches_eddington_inversion():
+    """The Osipkov-Merritt f(Q) of nsg_generate_om against a numerical Eddington
+    inversion of rho_Q = (1 + r^2/r_a^2) rho (ics._om_df_table)."""
+    Q = np.array([0.05, 0.1, 0.2, 0.4, 0.6, 0.8])
+    for r_a in (0.75, 1.0, 3.0):
+        Qt, ft = ics._om_df_table(r_a)
+        want = np.interp(Q, Qt, ft)
+        got = ics.hernquist_df(Q) + np.sqrt(Q) * (1 - 2 * Q) / (np.sqrt(2) * np.pi ** 3 * r_a ** 2)
+        np.testing.assert_allclose(got, want, rtol=2e-3)
+
+
+def test_om_restatement_has_the_model_anisotropy():
+    r_a = 1.0
+    r, vr, ell, ids, mu = ics.hernquist_om_counter(300_000, seed=9, r_max=100.0, r_a=r_a)
+    m = (r / (1 + r)) ** 2 / (100.0 / 101.0) ** 2
+    assert abs(np.sort(m) - (np.arange(m.size) + 0.5) / m.size).max() < 5e-3
+    # beta(r) = 1 - <v_t^2> / (2 <v_r^2>) = r^2 / (r^2 + r_a^2) for Osipkov-Merritt
+    vt2 = (ell / r) ** 2
+    for lo, hi in ((0.1, 0.3), (0.8, 1.25), (3.0, 6.0)):
+        sel = (r > lo) & (r < hi)
+        beta = 1 - np.mean(vt2[sel]) / (2 * np.mean(vr[sel] ** 2))
+        rm = np.sqrt(lo * hi)
+        assert abs(beta - rm ** 2 / (rm ** 2 + r_a ** 2)) < 0.05, (lo, hi, beta)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("r_a,n", [(1.0, 150_001), (2.5, 20_000)])
+def test_gpu_om_generator_matches_restatement(nsg, r_a, n):
+    seed = 17
+    with nsg.Context(nsg.default_params(carry_aux=1)) as c:
+        c.generate_om(n, seed, 100.0, r_a)
+        assert c.status() & nsg.ST_IC_REJECT == 0
+        r, vr, ell, ids, mu = c.download(with_aux=True)
+    want = ics.hernquist_om_counter(n, seed, 100.0, r_a)
+    assert np.array_equal(ids, np.arange(n))
+    for got, w in zip((r, vr, ell, mu), (want[0], want[1], want[2], want[4])):
+        assert np.array_equal(got, w)

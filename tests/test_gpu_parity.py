@@ -438,3 +438,20 @@ def test_step_download_equals_step_then_download(nsg, method):
                 outs.append(c.download())
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
+
+
+def test_config1_full_run_matches_oracle(nsg, oracle):
+    """The whole fixed-step configuration: N = 1e5 Plummer, dt = 1e-3, 1000 KDK steps,
+    bit for bit against the oracle (which the reference's functions pin)."""
+    n, steps = 100_000, 1000
+    r0, v0, l0, i0 = oracle.sort(*ics.plummer(n, seed=1))
+    p = oracle.params(dt=1e-3)
+    cur = (r0, v0, l0, i0)
+    for _ in range(steps):
+        cur = oracle.step_kdk(p, *cur)
+    with _ctx(nsg, dt=1e-3, method=nsg.METHOD_KDK) as c:
+        c.upload(r0, v0, l0, i0)
+        c.step(steps)
+        r, vr, ell, ids = c.download()
+        assert c.status() == 0
+    assert np.array_equal(ids, cur[3]) and np.array_equal(r, cur[0]) and np.array_equal(vr, cur[1])

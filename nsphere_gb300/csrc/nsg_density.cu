@@ -791,6 +791,25 @@ extern "C" int nsg_post_snapshot(nsg_ctx *c, const void *records, int64_t n, nsg
     if (int rc = sort_state(c)) return rc;
     const int k = c->cur;
     const double *R = c->r[k], *V = c->vr[k], *L = c->ell[k];
+    // the knot adjustment (one warp, the longest stage) runs on the side stream
+    // beside the density and the potential
+    e = cudaEventRecord(c->ev_fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+    if (e != cudaSuccess) return cuda_err(c, e, "post-processing fork");
+    {
+        ProfScope ps(c, "post_knots", (double)n * 16, c->side);
+        k_psi_knots<<<1, 32, 0, c->side>>>(R, n, knots);
+        c->launches += 1;
+    }
+    e = cudaEventRecord(c->ev_join, c->side);
+    if (e != cudaSuccess) return cuda_err(c, e, "post-processing join");
+    // on every return from here the buffers are freed on the main stream (B's
+    // destructor) only after the side stream's warp is done with them
+    struct JoinGuard {
+        cudaStream_t st;
+        cudaEvent_t ev;
+        ~JoinGuard() { cudaStreamWaitEvent(st, ev, 0); }
+    } join_guard{s, c->ev_join};
     {
         ProfScope ps(c, "post_density", (double)n * 24);
         if (int rc = density(c, R, n, rho)) return rc;
@@ -802,11 +821,8 @@ extern "C" int nsg_post_snapshot(nsg_ctx *c, const void *records, int64_t n, nsg
         k_set_psi0<<<1, 1, 0, s>>>(psiK, total, c->p.G, dM);
         c->launches += 1;
     }
-    {
-        ProfScope ps(c, "post_knots", (double)n * 16);
-        k_psi_knots<<<1, 32, 0, s>>>(R, n, knots);
-        c->launches += 1;
-    }
+    e = cudaStreamWaitEvent(s, c->ev_join, 0);
+    if (e != cudaSuccess) return cuda_err(c, e, "post-processing join");
     {
         ProfScope ps(c, "post_interp", (double)n * 48);
         k_psi_interp<<<grid_for(c, n, 256), 256, 0, s>>>(knots, psiK, n + 1, R, nullptr, n, psiS);

@@ -455,3 +455,20 @@ def test_config1_full_run_matches_oracle(nsg, oracle):
         r, vr, ell, ids = c.download()
         assert c.status() == 0
     assert np.array_equal(ids, cur[3]) and np.array_equal(r, cur[0]) and np.array_equal(vr, cur[1])
+
+
+def test_step_download_carries_aux(nsg):
+    n = 30000
+    r, vr, ell, ids = _adaptive_case(n, 53, lowl=100)
+    mu = np.random.default_rng(3).uniform(-1, 1, n)
+    outs = []
+    for overlapped in (False, True):
+        with _ctx(nsg, dt=1e-3, max_subdiv=64, lc_rule=1, lc_radius=5e-2, carry_aux=1) as c:
+            c.upload(r, vr, ell, ids, mu)
+            if overlapped:
+                outs.append(c.step_download(2, with_aux=True))
+            else:
+                c.step(2)
+                outs.append(c.download(with_aux=True))
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)

@@ -131,7 +131,8 @@ def _compare(srt, uns, psi0, want, rec, M):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,nan,ties,M,G", [(200_003, 20, 500, 1.0, 1.0), (60_000, 0, 0, 2.5, 0.7)])
+@pytest.mark.parametrize("n,nan,ties,M,G", [(200_003, 20, 500, 1.0, 1.0), (60_000, 0, 0, 2.5, 0.7),
+                                           (250, 0, 0, 1.0, 1.0), (30_001, 0, 3000, 1.0, 1.0)])
 def test_post_snapshot_matches_oracle(nsg, oracle, n, nan, ties, M, G):
     rec = _records(n, 31 + n % 7, nan=nan, ties=ties)
     want = oracle.post_snapshot(rec["r"], rec["v"], rec["l"], G=G, M=M)

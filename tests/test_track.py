@@ -142,3 +142,24 @@ def test_recorder_bad_ids_and_reopen(nsg):
             c.track_read()
         with pytest.raises(nsg.NsgError):
             c.track_open(np.array([1], dtype=np.int32), nsg.Psi(7, 0, 1.0, 0.0, 0.0, 0.0), capacity=1)
+
+
+@pytest.mark.gpu
+def test_recorder_equals_gather_on_an_ensemble(nsg):
+    """Ids are global over the halos of an ensemble: the recorder's r, v_r, ell after
+    each step equal nsg_gather's for the same ids."""
+    r, vr, ell, ids, sizes = ics.plummer_ensemble(4, 2000, 8000, seed=5)
+    track = np.array([0, 5, int(sizes[0]) + 3, int(ids.size) - 1], dtype=np.int32)
+    with nsg.Context(nsg.default_params(dt=1e-3, max_subdiv=64, lc_rule=1, lc_radius=1e-2)) as c:
+        c.upload_ensemble(r, vr, ell, ids, sizes)
+        c.track_open(track, nsg.Psi(1, 0, 1.0, 0.0, 0.0, 0.0), capacity=4)
+        want = []
+        for _ in range(4):
+            c.step(1)
+            gr, gv, gl, _ = c.gather(track)
+            want.append((gr, gv, gl))
+        got, seen = c.track_read()
+    assert seen == 4
+    for s, (gr, gv, gl) in enumerate(want):
+        assert np.array_equal(got[0, :, s], gr) and np.array_equal(got[1, :, s], gv)
+        assert np.array_equal(got[2, :, s], gl)

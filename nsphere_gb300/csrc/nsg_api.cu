@@ -309,6 +309,9 @@ static int check_params(nsg_ctx *c, const nsg_params *p)
     if (p->out_type < 0 || p->out_type > 2) return set_err(c, NSG_EINVAL, "out_type must be 0, 1 or 2");
     if (p->lc_rule < 0 || p->lc_rule > 2) return set_err(c, NSG_EINVAL, "unknown lc_rule");
     if (p->max_tau_steps < 0) return set_err(c, NSG_EINVAL, "max_tau_steps must be >= 0");
+    // the integrators compare against these on the integer pipe, which needs them to be numbers
+    if (isnan(p->tol_r) || isnan(p->tol_v) || isnan(p->lc_radius) || isnan(p->lc_alpha))
+        return set_err(c, NSG_EINVAL, "tolerances, lc_radius and lc_alpha must not be NaN");
     if (p->sched != NSG_SCHED_PLAIN && p->sched != NSG_SCHED_LEARNED) return set_err(c, NSG_EINVAL, "unknown sched");
     return NSG_OK;
 }

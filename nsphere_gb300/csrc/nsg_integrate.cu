@@ -95,9 +95,9 @@ template <bool HW>
 __device__ __forceinline__ bool converged(double rc, double vc, double rf, double vf,
                                           double rscale, double tol_r, double tol_v)
 {
-    double dr = ddivx<HW>(fabs(dsub(rf, rc)), dadd(fabs(rscale), 1.0e-30));
-    double dv = ddivx<HW>(fabs(dsub(vf, vc)), dadd(fabs(vf), 1.0e-30));
-    return (dr < tol_r) && (dv < tol_v);
+    double dr = ddivx<HW>(iabs(dsub(rf, rc)), dadd(iabs(rscale), 1.0e-30));
+    double dv = ddivx<HW>(iabs(dsub(vf, vc)), dadd(iabs(vf), 1.0e-30));
+    return abs_lt(dr, tol_r) && abs_lt(dv, tol_v);   // dr, dv >= +0 or NaN; tolerances are numbers
 }
 
 __device__ __forceinline__ void select_out(int out_type, double rc, double vc, double rf,
@@ -116,20 +116,20 @@ __device__ __forceinline__ bool route_lc(const StepArgs &a, const Local &L, doub
 {
     if ((a.method != NSG_METHOD_ADAPTIVE_LC && a.method != NSG_METHOD_FULL_LC) || a.lc_rule == NSG_LC_OFF)
         return false;
-    if (a.lc_rule == NSG_LC_RADIUS) return (r > 1.0e-30) && (r < a.lc_radius);
+    if (a.lc_rule == NSG_LC_RADIUS) return open_between(r, 1.0e-30, a.lc_radius);
     double r_crit = 0.0;
     if (a.method == NSG_METHOD_FULL_LC) {
         // method 4 (nsphere.c:5696-5707): M_i = (i/N) M for every rank, any ell != 0
         if (ell != 0.0) {
-            const double gravPart = dmul(a.G, dmul(ddiv((double)L.i, (double)L.n), a.M));
+            const double gravPart = dmul(a.G, dmul(ddiv(u32_to_double((uint32_t)L.i), u32_to_double((uint32_t)L.n)), a.M));
             r_crit = ddiv(dmul(dmul(ell, ell), a.lc_alpha), gravPart);
         }
         return (r > 1.0e-30) && (r < r_crit);
     }
     if (fabs(ell) > 1.0e-30) {
         double M_enc;
-        if (L.i == 0) M_enc = dmul(dmul(0.1, ddiv(1.0, (double)L.n)), a.M);
-        else M_enc = dmul(ddiv((double)L.i, (double)L.n), a.M);
+        if (L.i == 0) M_enc = dmul(dmul(0.1, ddiv(1.0, u32_to_double((uint32_t)L.n))), a.M);
+        else M_enc = dmul(ddiv(u32_to_double((uint32_t)L.i), u32_to_double((uint32_t)L.n)), a.M);
         double gravPart = dmul(a.G, M_enc);
         r_crit = ddiv(dmul(dmul(ell, ell), a.lc_alpha), gravPart);
     }
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(512) k_gather_level0(StepArgs a)
             micro_leap<false>(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
             micro_leap<false>(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
             const bool ok = converged<false>(rc, vc, rf, vf, rf, a.tol_r, a.tol_v);
-            const bool bad = !(isfinite(rf) && isfinite(vf));
+            const bool bad = !(finite_bits(rf) && finite_bits(vf));
             done = ok || last || (bad && a.nf_stop);
             if (done) {
                 double ro, vo;
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
                 const double vC = (!FULL && kcheck == 1) ? vq : vC0;
                 if (active && kcheck >= kstart) {
                     const bool ok = converged<true>(rC, vC, rF, vF, rF, a.tol_r, a.tol_v);
-                    const bool bad = !(isfinite(rF) && isfinite(vF));
+                    const bool bad = !(finite_bits(rF) && finite_bits(vF));
                     if (ok || (bad && a.nf_stop) || kcheck == nl) {
                         if (j == 0) {
                             double ro, vo;
@@ -421,9 +421,9 @@ template <bool FAST>
 __device__ __forceinline__ bool lc_converged(double rc, double vc, double rf, double vf, double rscale,
                                              double tol_r, double tol_v, bool &bad)
 {
-    const double dr = lc_div<FAST>(fabs(dsub(rf, rc)), dadd(fabs(rscale), 1.0e-30), bad);
-    const double dv = lc_div<FAST>(fabs(dsub(vf, vc)), dadd(fabs(vf), 1.0e-30), bad);
-    return (dr < tol_r) && (dv < tol_v);
+    const double dr = lc_div<FAST>(iabs(dsub(rf, rc)), dadd(iabs(rscale), 1.0e-30), bad);
+    const double dv = lc_div<FAST>(iabs(dsub(vf, vc)), dadd(iabs(vf), 1.0e-30), bad);
+    return abs_lt(dr, tol_r) && abs_lt(dv, tol_v);
 }
 
 // Slots of each lane's pass in a tau-step record of radii (PAIR form): lane 0 the

@@ -154,6 +154,41 @@ namespace nsg {
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+
+// Predicates and exact conversions on the integer pipe.  On GB300 every FP64
+// instruction -- a comparison or an int-to-double conversion included -- occupies the
+// FP64 pipe, which the throughput kernels saturate, so they test bit patterns instead.
+// The bit pattern comes out of an asm move, opaque to the compiler: given the plain
+// reinterpretation, it turns the masked integer compare of abs_lt back into a
+// floating-point compare, with a wrong answer for NaN (true for |NaN| < y).
+__device__ __forceinline__ long long dbits(double x)
+{
+    long long b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+    return b;
+}
+// isfinite(x)
+__device__ __forceinline__ bool finite_bits(double x) { return ((dbits(x) >> 52) & 0x7ff) != 0x7ff; }
+// fabs(x) for a number (a NaN comes out with its sign cleared; fabs keeps it on GB300)
+__device__ __forceinline__ double iabs(double x) { return __longlong_as_double(dbits(x) & 0x7fffffffffffffffll); }
+// |x| < y for y not NaN (signed-integer order of the bit patterns is the order of
+// non-negative doubles, and a negative y sorts below every |x|)
+__device__ __forceinline__ bool abs_lt(double x, double y) { return (dbits(x) & 0x7fffffffffffffffll) < dbits(y); }
+// lo < r < hi for lo >= +0 and hi not NaN; false for a NaN r, as the floating-point test
+__device__ __forceinline__ bool open_between(double r, double lo, double hi)
+{
+    const long long b = dbits(r);
+    return b > dbits(lo) && b < dbits(hi);
+}
+// x as a double, exactly, for 0 <= x < 2^32
+__device__ __forceinline__ double u32_to_double(uint32_t x)
+{
+    if (x == 0u) return 0.0;
+    const int e = 31 - __clz((int)x);
+    const unsigned long long m = ((unsigned long long)x << (52 - e)) & 0x000fffffffffffffull;
+    return __longlong_as_double((long long)((((unsigned long long)(1023 + e)) << 52) | m));
+}
+
 // Division: throughput-bound kernels divide on the integer/FP32 pipes
 // (div_rn, nsg_div.cuh); the Levi-Civita chains use the latency-oriented
 // div_rn_lat with the FP64 pipe's division as its fallback.  All are IEEE
@@ -166,7 +201,7 @@ __device__ __forceinline__ double ddiv(double a, double b) { return div_rn(a, b)
 template <bool HW = false>
 __device__ __forceinline__ double gnum_of(int64_t i, int64_t n, double G, double M, double Mpt)
 {
-    double g = dmul(dmul(-G, ddivx<HW>((double)i, (double)n)), M);
+    double g = dmul(dmul(-G, ddivx<HW>(u32_to_double((uint32_t)i), u32_to_double((uint32_t)n))), M);
     if (Mpt != 0.0) g = dsub(g, dmul(G, Mpt));
     return g;
 }
@@ -182,8 +217,9 @@ __device__ __forceinline__ double acc_leap(double r, double gnum, double l2)
 // Order-preserving map of a double to uint64: -0.0 -> +0.0, NaN -> all ones.
 __device__ __forceinline__ uint64_t radius_key(double r)
 {
-    if (r != r) return ~0ull;
-    unsigned long long u = (r == 0.0) ? 0ull : (unsigned long long)__double_as_longlong(r);
+    unsigned long long u = (unsigned long long)dbits(r);
+    if ((u & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return ~0ull;   // NaN
+    if ((u << 1) == 0ull) u = 0ull;                                           // -0 -> +0
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 

@@ -71,14 +71,29 @@ NSG_HD double div_from_bits(uint64_t u)
 #endif
 }
 
+// x as a float for x in [2^23, 2^24), from its bits: exponent 23, the low 23 bits
+// as the fraction.  Exact, and one logic operation instead of a conversion.
+NSG_HD float div_f24(uint32_t x)
+{
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float((150u << 23) | (x & 0x7fffffu));
+#else
+    return (float)x;
+#endif
+}
+
 // Estimate of 2^76 / fb for fb in [2^23, 2^24) as an integer, relative error < 2^-21.
+// The estimate y lies in (2^-24, 2^-23], so y 2^76 is an integer of 53 or 54 bits:
+// its 24-bit significand shifted left by (biased exponent of y) - 74.  Building it
+// from the bits keeps a 64-bit conversion, which shares the FP64 pipe on GB300, out
+// of the integer division.
 NSG_HD int64_t div_recip_seed(uint32_t mb_top24)
 {
 #if defined(__CUDA_ARCH__)
-    float fb = (float)mb_top24;  // exact: fewer than 25 significant bits
     float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(fb));
-    return (int64_t)__float2ll_rz(y * 0x1p76f);
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(div_f24(mb_top24)));
+    const uint32_t fy = __float_as_uint(y);
+    return (int64_t)((fy & 0x7fffffu) | 0x800000u) << ((int)(fy >> 23) - 74);
 #else
     float fb = (float)mb_top24;
     float y = 1.0f / fb;
@@ -140,19 +155,33 @@ NSG_HD bool div_rn_fast(double a, double b, double *out)
 // ---------------------------------------------------------------------------
 // Latency-oriented division for serial chains (one particle's Levi-Civita
 // substeps).  On GB300 a dependent FP64 operation takes 64 cycles and the FP64
-// division about 590; this routine takes about 220 on the integer and FP32 pipes.
+// division about 590; this routine runs on the integer and FP32 pipes, with no
+// conversion instruction on its dependent path.
 //
 // Method (digit recurrence with an approximate reciprocal and exact remainders):
-//   A = ma or 2 ma so that A/mb lies in [1, 2);  ys ~ 2^48/mb in single precision
-//   from rcp.approx of the top 24 bits of mb (relative error < 2^-21);
-//   q1 = round(float(A >> 26) ys)            ~ A 2^22 / mb,  r1 = A 2^22 - q1 mb
-//   q2 = round(float(r1 >> 28) 4 ys)         ~ r1 2^22 / mb, r2 = r1 2^22 - q2 mb
-//   q3 = round(float(r2 >> 28) 2^-11 ys)     ~ r2 2^9 / mb,  r3 = r2 2^9 - q3 mb
-//   Q = q1 2^31 + q2 2^9 + q3 satisfies A 2^53 = Q mb + r3 exactly.  Each
-//   remainder is computed modulo 2^64; its true value is below 2^58 in magnitude
-//   (each digit is within a few units of its ideal value), so the modular result
-//   is exact.  |r3| < mb/2, so one step (r3 < 0: Q - 1, r3 + mb) makes Q the floor
-//   and 0 <= r3 < mb the exact remainder: round bit Q & 1, sticky r3 != 0.
+//   A = ma or 2 ma so that A/mb lies in [1, 2);  y ~ 2^29/mb in single precision
+//   from rcp.approx of the top 24 bits of mb; s_j = y 2^(k_j + d_j - 29) (exact).
+//   Digit j: t = float(r >> k_j), exact; q_j = round(t s_j) ~ r 2^(d_j) / mb;
+//   the next remainder r 2^(d_j) - q_j mb.  With (d, k) = (21, 31), (18, 35),
+//   (14, 34) from r = A:
+//     q1 ~ A 2^21 / mb,  r1 = A 2^21 - q1 mb
+//     q2 ~ r1 2^18 / mb, r2 = r1 2^18 - q2 mb
+//     q3 ~ r2 2^14 / mb, r3 = r2 2^14 - q3 mb
+//   and Q = q1 2^32 + q2 2^14 + q3 satisfies A 2^53 = Q mb + r3 exactly.
+//   Conversions use magic numbers: an integer below 2^23 (or of magnitude below
+//   2^22) placed in the fraction of 2^23 (1.5 2^23) minus that constant is the
+//   integer as a float, exactly; fma(t, s, 2^23) (1.5 2^23) rounds t s to the
+//   nearest integer in one rounding, read back from the fraction bits.
+// Error bounds.  With the estimate's relative error e (truncation of mb to 24
+// bits and rcp.approx: below 2^-22; below 10 2^-23 for the host tests that
+// perturb it by 8 ulps), digit j misses its ideal value by at most
+//   1/2 + 2^(k_j + d_j - 52) + |r| 2^(d_j) e / mb:
+//   digit 1 by 11.5 at most, so |r1| < 11.5 mb < 2^56.6 and |r1 >> 35| < 2^22;
+//   digit 2 by 1/2 + 2 + 11.5 2^18 e < 6.1, so |r2| < 2^55.7 and |r2 >> 34| < 2^22;
+//   digit 3 by 1/2 + 2^-4 + 6.1 2^14 e < 0.69, so |r3| < mb.
+// Every remainder is far below 2^63, so its value modulo 2^64 is exact, and one
+// step (r3 < 0: Q - 1, r3 + mb) makes Q the floor and 0 <= r3 < mb the exact
+// remainder: round bit Q & 1, sticky r3 != 0.
 // There are no branches: every operand runs the same instructions, and `ok` says
 // whether the result stands (both operands normal, or a +-0 dividend over a normal
 // divisor, and a normal quotient); otherwise the caller divides in hardware.  A
@@ -162,7 +191,7 @@ NSG_HD float div_lat_rcp(int32_t x)
 {
 #if defined(__CUDA_ARCH__)
     float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(__int2float_rn(x)));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(div_f24((uint32_t)x)));   // x in [2^23, 2^24)
     return y;
 #elif defined(NSG_DIV_HOST_RCP)
     return NSG_DIV_HOST_RCP(x);   // host tests substitute perturbed estimates
@@ -171,13 +200,58 @@ NSG_HD float div_lat_rcp(int32_t x)
 #endif
 }
 
-NSG_HD int32_t div_lat_digit(int32_t top, float scale)
+NSG_HD float div_fbits(uint32_t u)
 {
 #if defined(__CUDA_ARCH__)
-    return __float2int_rn(__int2float_rn(top) * scale);
+    return __uint_as_float(u);
 #else
-    return (int32_t)__builtin_nearbyintf((float)top * scale);
+    float f;
+    __builtin_memcpy(&f, &u, 4);
+    return f;
 #endif
+}
+
+NSG_HD uint32_t div_ubits(float f)
+{
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    __builtin_memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+
+NSG_HD float div_fsub(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+
+NSG_HD float div_ffma(float a, float b, float c)
+{
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return __builtin_fmaf(a, b, c);
+#endif
+}
+
+// First digit: t = x for 0 <= x < 2^23; round(t s) for 0 <= t s < 2^23 - 1/2.
+NSG_HD uint32_t div_lat_digit_u(uint32_t x, float s)
+{
+    const float t = div_fsub(div_fbits(0x4B000000u | x), 8388608.0f);
+    return div_ubits(div_ffma(t, s, 8388608.0f)) - 0x4B000000u;
+}
+
+// Later digits: t = x for |x| < 2^22; round(t s) for |t s| < 2^22 - 1/2.
+NSG_HD int32_t div_lat_digit_s(int32_t x, float s)
+{
+    const float t = div_fsub(div_fbits(0x4B400000u + (uint32_t)x), 12582912.0f);
+    return (int32_t)(div_ubits(div_ffma(t, s, 12582912.0f)) - 0x4B400000u);
 }
 
 NSG_HD double div_rn_lat(double a, double b, bool &ok)
@@ -192,14 +266,14 @@ NSG_HD double div_rn_lat(double a, double b, bool &ok)
     const bool lt = ma < mb;
     const uint64_t A = lt ? ma << 1 : ma;
     const int32_t e = (int32_t)ea - (int32_t)eb + 1023 - (lt ? 1 : 0);
-    const float ys = div_lat_rcp((int32_t)(mb >> 29)) * 0x1p19f;
-    const int32_t q1 = div_lat_digit((int32_t)(A >> 26), ys);
-    const int64_t r1 = (int64_t)((A << 22) - (uint64_t)(int64_t)q1 * mb);
-    const int32_t q2 = div_lat_digit((int32_t)(r1 >> 28), ys * 4.0f);
-    const int64_t r2 = (int64_t)(((uint64_t)r1 << 22) - (uint64_t)(int64_t)q2 * mb);
-    const int32_t q3 = div_lat_digit((int32_t)(r2 >> 28), ys * 0x1p-11f);
-    const int64_t r3 = (int64_t)(((uint64_t)r2 << 9) - (uint64_t)(int64_t)q3 * mb);
-    const int64_t Q = ((int64_t)q1 << 31) + ((int64_t)q2 << 9) + (int64_t)q3;
+    const float y = div_lat_rcp((int32_t)(mb >> 29));
+    const uint32_t q1 = div_lat_digit_u((uint32_t)(A >> 31), y * 0x1p23f);
+    const int64_t r1 = (int64_t)((A << 21) - (uint64_t)q1 * mb);
+    const int32_t q2 = div_lat_digit_s((int32_t)(r1 >> 35), y * 0x1p24f);
+    const int64_t r2 = (int64_t)(((uint64_t)r1 << 18) - (uint64_t)(int64_t)q2 * mb);
+    const int32_t q3 = div_lat_digit_s((int32_t)(r2 >> 34), y * 0x1p19f);
+    const int64_t r3 = (int64_t)(((uint64_t)r2 << 14) - (uint64_t)(int64_t)q3 * mb);
+    const int64_t Q = ((int64_t)q1 << 32) + ((int64_t)q2 << 14) + (int64_t)q3;
     const bool neg = r3 < 0;
     const int64_t rr = neg ? r3 + (int64_t)mb : r3;
     const uint64_t Qc = (uint64_t)(neg ? Q - 1 : Q);

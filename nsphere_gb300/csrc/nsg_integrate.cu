@@ -95,8 +95,8 @@ template <bool HW>
 __device__ __forceinline__ bool converged(double rc, double vc, double rf, double vf,
                                           double rscale, double tol_r, double tol_v)
 {
-    double dr = ddivx<HW>(iabs(dsub(rf, rc)), dadd(iabs(rscale), 1.0e-30));
-    double dv = ddivx<HW>(iabs(dsub(vf, vc)), dadd(iabs(vf), 1.0e-30));
+    double dr = ddivx<HW>(iabs(dsub(rf, rc)), add_1em30(iabs(rscale)));
+    double dv = ddivx<HW>(iabs(dsub(vf, vc)), add_1em30(iabs(vf)));
     return abs_lt(dr, tol_r) && abs_lt(dv, tol_v);   // dr, dv >= +0 or NaN; tolerances are numbers
 }
 
@@ -106,8 +106,8 @@ __device__ __forceinline__ void select_out(int out_type, double rc, double vc, d
     if (out_type == 0) { ro = rc; vo = vc; }
     else if (out_type == 1) { ro = rf; vo = vf; }
     else {
-        ro = dsub(dmul(4.0, rf), dmul(3.0, rc));
-        vo = dsub(dmul(4.0, vf), dmul(3.0, vc));
+        ro = dsub(mul4(rf), dmul(3.0, rc));
+        vo = dsub(mul4(vf), dmul(3.0, vc));
     }
 }
 

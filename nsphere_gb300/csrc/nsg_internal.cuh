@@ -180,6 +180,21 @@ __device__ __forceinline__ bool open_between(double r, double lo, double hi)
     const long long b = dbits(r);
     return b > dbits(lo) && b < dbits(hi);
 }
+// x + 1e-30 for x >= +0 or NaN.  From x = 2^-46 up, 1e-30 is below half an ulp of x
+// (2^-99), so the sum rounds to x; only smaller x take the FP64 addition.
+__device__ __forceinline__ double add_1em30(double x)
+{
+    if (dbits(x) >= (977ll << 52)) return x;
+    return dadd(x, 1.0e-30);
+}
+// 4 x: for a normal x whose product stays normal the exponent field rises by two
+// (exact, as the multiplication); other x take the FP64 multiplication.
+__device__ __forceinline__ double mul4(double x)
+{
+    const long long b = dbits(x);
+    if (((unsigned)(b >> 52) & 0x7ffu) - 1u < 2044u) return __longlong_as_double(b + (2ll << 52));
+    return dmul(4.0, x);
+}
 // x as a double, exactly, for 0 <= x < 2^32
 __device__ __forceinline__ double u32_to_double(uint32_t x)
 {

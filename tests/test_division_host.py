@@ -18,7 +18,7 @@ def checker(tmp_path_factory):
     return exe
 
 
-@pytest.mark.parametrize("ulps", [0, 2, -2, 4, -4])
+@pytest.mark.parametrize("ulps", [0, 2, -2, 4, -4, 8, -8, 16])
 def test_division_matches_ieee(checker, ulps):
     out = subprocess.run([checker, str(ulps), "1500000"], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr

@@ -311,10 +311,12 @@ int nsg_status(nsg_ctx *ctx, uint32_t *flags);
 int nsg_clear_status(nsg_ctx *ctx);
 
 /* Diagnostic without a reference counterpart: compares the library's integer-pipe
- * double division (used by every integrator in place of the FP64 pipe's) with the
- * hardware IEEE division on `count` generated operand pairs on the current device.
- * mismatches must come back 0; fast_path counts pairs that took the integer path;
- * first_bad[0..1] receives the first mismatching (a, b). */
+ * double divisions (used by every integrator in place of the FP64 pipe's) with the
+ * hardware IEEE division on `count` generated operand pairs on the current device,
+ * and its division-free test RN(|a|/|b|) < tol (the integrators' acceptance tests)
+ * with the divided quotient, for tol at, one ulp either side of, and away from the
+ * quotient.  mismatches must come back 0; fast_path counts pairs that took the
+ * integer path; first_bad[0..1] receives the first mismatching (a, b). */
 int nsg_selftest_division(uint64_t seed, int64_t count, int64_t *mismatches,
                           int64_t *fast_path, double *first_bad);
 
@@ -332,7 +334,9 @@ int nsg_probe_fp64(double *dfma_tflops, double *div_hw_gps, double *div_int_gps,
  * [6] 32-bit integer multiply-add; [7] 64-bit multiply-high; [8] int->float, multiply,
  * float->int; [9] one Levi-Civita substep of the leading warp (split force); [10] the
  * same with a zero gravity numerator; [11] the same with both force quotients in
- * every lane (no exchange).  count = how many to measure (<= 12). */
+ * every lane (no exchange); [12] dadd of a value and its copy from the other half of
+ * the warp (shuffle); [13] dadd, then a 64-bit select by lane half.  count = how many
+ * to measure (<= 14). */
 int nsg_probe_latency(double *cycles, int count);
 
 /* ---- learned level scheduler (no reference counterpart: an addition of this

@@ -495,7 +495,7 @@ def probe_fp64() -> dict:
 LATENCY_PROBES = ["fp64_fma", "fp64_fma_two_chains_one_warp", "fp64_fma_one_chain_two_warps",
                   "div_fp64_pipe", "div_int_throughput_form", "div_latency_form", "imad32", "mulhi64",
                   "i2f_fmul_f2i", "levi_civita_substep", "levi_civita_substep_zero_gravity",
-                  "levi_civita_substep_both_quotients"]
+                  "levi_civita_substep_both_quotients", "dadd_shuffle_half_warp", "dadd_select_f64"]
 
 
 def probe_latency() -> dict:

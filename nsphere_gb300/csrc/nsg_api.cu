@@ -235,6 +235,23 @@ __global__ void k_selftest_div(uint64_t seed, int64_t count, unsigned long long 
         const double ql = div_rn_lat(a, b, ok_l), zl = div_rn_lat(z, b, ok_z);
         if (ok_l) same = same && (__double_as_longlong(ql) == __double_as_longlong(t));
         if (ok_z) same = same && (__double_as_longlong(zl) == __double_as_longlong(zt));
+        // the comparison RN(x/y) < tol without division, for tolerances at the quotient,
+        // one ulp either side of it, and at a random normal number
+        {
+            const double x = fabs(a), y = fabs(b), qt = __ddiv_rn(x, y);
+            const long long bq = __double_as_longlong(qt);
+            double tol;
+            switch ((h3 >> 50) & 3) {
+            case 0: tol = qt; break;
+            case 1: tol = __longlong_as_double(bq + 1); break;
+            case 2: tol = __longlong_as_double(bq - 1); break;
+            default: tol = __longlong_as_double((long long)((h1 ^ h2) & 0x7fefffffffffffffull)); break;
+            }
+            const RatioBound rb = ratio_bound(tol);
+            bool dec;
+            const bool lt = ratio_lt(x, y, rb, dec);
+            if (dec) same = same && (lt == (qt < tol));
+        }
         if (!same && atomicAdd(&out[1], 1ull) == 0) { first[0] = a; first[1] = b; }
     }
     atomicAdd(&out[2], fast);

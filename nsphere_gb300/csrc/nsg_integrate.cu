@@ -47,6 +47,7 @@ struct StepArgs {
     int8_t *level;
     int64_t n;
     double G, M, dt, tol_r, tol_v;
+    RatioBound rb_r, rb_v;      // the tolerances' midpoints below (ratio_lt)
     int nlev;                   // number of levels: floor(log2(max_subdiv)) + 1
     int out_type;
     int method;
@@ -91,13 +92,21 @@ __device__ __forceinline__ void micro_leap(double r, double v, double l2, double
 
 // Acceptance test of nsphere.c:1688-1691 (and :2125-2128, whose radius term is
 // scaled by rF^2 instead of rF).
+// The quotients are only compared with the tolerances, so ratio_lt decides each test
+// from the operands' bits; the division runs for the operands it leaves undecided.
 template <bool HW>
 __device__ __forceinline__ bool converged(double rc, double vc, double rf, double vf,
-                                          double rscale, double tol_r, double tol_v)
+                                          double rscale, const StepArgs &a)
 {
-    double dr = ddivx<HW>(iabs(dsub(rf, rc)), add_1em30(iabs(rscale)));
-    double dv = ddivx<HW>(iabs(dsub(vf, vc)), add_1em30(iabs(vf)));
-    return abs_lt(dr, tol_r) && abs_lt(dv, tol_v);   // dr, dv >= +0 or NaN; tolerances are numbers
+    const double xr = iabs(dsub(rf, rc)), yr = add_1em30(iabs(rscale));
+    const double xv = iabs(dsub(vf, vc)), yv = add_1em30(iabs(vf));
+    bool dec_r, dec_v;
+    bool ok_r = ratio_lt(xr, yr, a.rb_r, dec_r);
+    bool ok_v = ratio_lt(xv, yv, a.rb_v, dec_v);
+    // dr, dv >= +0 or NaN; the tolerances are numbers
+    if (!dec_r) ok_r = abs_lt(ddivx<HW>(xr, yr), a.tol_r);
+    if (!dec_v) ok_v = abs_lt(ddivx<HW>(xv, yv), a.tol_v);
+    return ok_r && ok_v;
 }
 
 __device__ __forceinline__ void select_out(int out_type, double rc, double vc, double rf,
@@ -170,7 +179,7 @@ __global__ void __launch_bounds__(512) k_gather_level0(StepArgs a)
         if (!fresh) {
             micro_leap<false>(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
             micro_leap<false>(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
-            const bool ok = converged<false>(rc, vc, rf, vf, rf, a.tol_r, a.tol_v);
+            const bool ok = converged<false>(rc, vc, rf, vf, rf, a);
             const bool bad = !(finite_bits(rf) && finite_bits(vf));
             done = ok || last || (bad && a.nf_stop);
             if (done) {
@@ -270,7 +279,7 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
                 const double rC = (!FULL && kcheck == 1) ? rq : rC0;
                 const double vC = (!FULL && kcheck == 1) ? vq : vC0;
                 if (active && kcheck >= kstart) {
-                    const bool ok = converged<true>(rC, vC, rF, vF, rF, a.tol_r, a.tol_v);
+                    const bool ok = converged<true>(rC, vC, rF, vF, rF, a);
                     const bool bad = !(finite_bits(rF) && finite_bits(vF));
                     if (ok || (bad && a.nf_stop) || kcheck == nl) {
                         if (j == 0) {
@@ -1015,6 +1024,7 @@ static StepArgs make_args(nsg_ctx *c)
     a.n = c->n;
     a.G = c->p.G; a.M = c->p.M_total; a.dt = c->p.dt;
     a.tol_r = c->p.tol_r; a.tol_v = c->p.tol_v;
+    a.rb_r = ratio_bound(a.tol_r); a.rb_v = ratio_bound(a.tol_v);
     int nlev = 0;
     for (int64_t N = 1; N <= c->p.max_subdiv && nlev < kMaxLevels - 1; N *= 2) nlev++;
     a.nlev = nlev;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -195,6 +196,50 @@ __device__ __forceinline__ double mul4(double x)
     if (((unsigned)(b >> 52) & 0x7ffu) - 1u < 2044u) return __longlong_as_double(b + (2ll << 52));
     return dmul(4.0, x);
 }
+// RN(x / y) < tol, decided without the division.  RN is monotonic, and the quotient
+// of two doubles is never halfway between two doubles (that would take a 54-bit odd
+// significand), so RN(x/y) < tol exactly when x/y lies below the midpoint between
+// tol and its predecessor: B 2^(e_t - 1076) with B = 2 m_t - 1, or B = 2^54 - 1 at
+// 2^(e_t - 1077) when tol is a power of two (m_t, e_t: significand and biased
+// exponent of tol).  With x = m_x 2^(e_x - 1075) and y = m_y 2^(e_y - 1075) that is
+// m_x 2^D < B m_y for D = e_x - e_y + doff: true for D <= 52 (left side below
+// 2^105), false for D >= 55 (left side at least 2^107), and one 64 x 64-bit product
+// for D = 53, 54.
+struct RatioBound {
+    uint64_t B;
+    int32_t doff;
+    int32_t ok;   // tol is a positive normal number
+};
+
+__host__ __device__ inline RatioBound ratio_bound(double tol)
+{
+    uint64_t b;
+    memcpy(&b, &tol, 8);
+    const uint32_t et = (uint32_t)(b >> 52) & 0x7ffu;
+    if ((b >> 63) != 0 || et == 0u || et == 0x7ffu) return RatioBound{0, 0, 0};
+    const uint64_t mt = (b & 0x000fffffffffffffull) | (1ull << 52);
+    if (mt == (1ull << 52)) return RatioBound{(1ull << 54) - 1ull, 1077 - (int32_t)et, 1};
+    return RatioBound{2ull * mt - 1ull, 1076 - (int32_t)et, 1};
+}
+
+// x >= +0 or NaN, y > 0 or NaN.  `decided` is false unless tol is a positive normal,
+// y is normal and x is +0 or normal; the caller then divides.
+__device__ __forceinline__ bool ratio_lt(double x, double y, const RatioBound &t, bool &decided)
+{
+    const long long bx = dbits(x), by = dbits(y);
+    const unsigned ex = (unsigned)(bx >> 52) & 0x7ffu, ey = (unsigned)(by >> 52) & 0x7ffu;
+    decided = t.ok && (ey - 1u < 2046u) && (bx == 0 || ex - 1u < 2046u);
+    if (bx == 0) return true;
+    const int D = (int)ex - (int)ey + t.doff;
+    if (D <= 52) return true;
+    if (D >= 55) return false;
+    const uint64_t mx = ((uint64_t)bx & 0x000fffffffffffffull) | (1ull << 52);
+    const uint64_t my = ((uint64_t)by & 0x000fffffffffffffull) | (1ull << 52);
+    const uint64_t rlo = t.B * my, rhi = __umul64hi(t.B, my);
+    const uint64_t llo = mx << D, lhi = mx >> (64 - D);
+    return lhi < rhi || (lhi == rhi && llo < rlo);
+}
+
 // x as a double, exactly, for 0 <= x < 2^32
 __device__ __forceinline__ double u32_to_double(uint32_t x)
 {

@@ -51,7 +51,8 @@ __global__ void k_probe_latency(double *out, long long *cyc, int iters, int kind
 // clock.  The asm statements pin the chains between the two clock reads.
 // kind: 0 DFMA chain; 1 two independent DFMA chains in one warp; 2 one DFMA chain in
 // each of two warps; 3 dadd + __ddiv_rn; 4 dadd + div_rn; 5 dadd + div_rn_lat;
-// 6 IMAD; 7 mul.hi.u64; 8 I2F + FMUL + F2I.
+// 6 IMAD; 7 mul.hi.u64; 8 I2F + FMUL + F2I; 12 dadd of x and its copy from the other
+// half-warp (shuffle); 13 dadd, then a 64-bit select by lane half.
 __global__ void k_probe_chain(double *out, long long *cyc, int iters, int kind)
 {
     const int t = threadIdx.x;
@@ -74,6 +75,14 @@ __global__ void k_probe_chain(double *out, long long *cyc, int iters, int kind)
     case 5: for (int i = 0; i < iters; i++) { bool o; x = div_rn_lat(0.7, __dadd_rn(x, 1.0), o); ok &= o; } break;
     case 6: for (int i = 0; i < iters; i++) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(w) : "r"(2654435761u), "r"(7u)); break;
     case 7: for (int i = 0; i < iters; i++) asm volatile("mul.hi.u64 %0, %0, %1;" : "+l"(u) : "l"(0xD1B54A32D192ED03ull)); break;
+    case 12: for (int i = 0; i < iters; i++) x = __dadd_rn(x, __shfl_xor_sync(0xffffffffu, x, 16)); break;
+    case 13:
+        for (int i = 0; i < iters; i++) {
+            const double z = __dadd_rn(x, 1e-9);
+            x = (t & 16) ? x : z;
+            asm volatile("" : "+d"(x));
+        }
+        break;
     default: for (int i = 0; i < iters; i++) w = __float2uint_rz(__uint2float_rz(w) * 0.999f) + 7u; break;
     }
     asm volatile("" : "+d"(x), "+d"(y), "+l"(u), "+r"(w));
@@ -93,11 +102,11 @@ extern "C" int nsg_probe_latency(double *cycles, int count)
     long long *cyc = nullptr;
     cudaError_t e = cudaMalloc((void **)&out, 64 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void **)&cyc, sizeof(long long));
-    const int n = count < 12 ? count : 12;
+    const int n = count < 14 ? count : 14;
     for (int k = 0; k < n && e == cudaSuccess; k++) {
         long long h = 0;
         const int it = 1024;
-        if (k <= 8) {
+        if (k <= 8 || k >= 12) {
             for (int rep = 0; rep < 2 && e == cudaSuccess; rep++) {
                 k_probe_chain<<<1, k == 2 ? 64 : 32>>>(out, cyc, it, k);
                 e = cudaDeviceSynchronize();

@@ -43,3 +43,56 @@ def test_recip_seed_from_float_bits():
     # the 24-bit divisor top as a float from its bits
     f24 = ((np.uint32(150) << np.uint32(23)) | (fb & np.uint32(0x7FFFFF))).view(np.float32)
     assert np.array_equal(f24, fb.astype(np.float32))
+
+
+def _ratio_bound(tol):
+    b = int(np.float64(tol).view(np.uint64))
+    et = (b >> 52) & 0x7FF
+    if (b >> 63) or et == 0 or et == 0x7FF:
+        return None
+    mt = (b & ((1 << 52) - 1)) | (1 << 52)
+    if mt == 1 << 52:
+        return (1 << 54) - 1, 1077 - et
+    return 2 * mt - 1, 1076 - et
+
+
+def _ratio_lt(x, y, rb):
+    """RN(x/y) < tol decided from the bits (ratio_lt); None where the kernel divides."""
+    bx, by = int(np.float64(x).view(np.uint64)), int(np.float64(y).view(np.uint64))
+    ex, ey = (bx >> 52) & 0x7FF, (by >> 52) & 0x7FF
+    if rb is None or not (1 <= ey <= 2046) or not (bx == 0 or 1 <= ex <= 2046):
+        return None
+    if bx == 0:
+        return True
+    B, doff = rb
+    D = ex - ey + doff
+    if D <= 52:
+        return True
+    if D >= 55:
+        return False
+    mx = (bx & ((1 << 52) - 1)) | (1 << 52)
+    my = (by & ((1 << 52) - 1)) | (1 << 52)
+    return (mx << D) < B * my   # the kernel's 128-bit comparison
+
+
+def test_ratio_test_matches_division():
+    rng = np.random.default_rng(3)
+    x = np.abs(_rand_doubles(rng, 20000, 800, 1200))
+    y = np.abs(_rand_doubles(rng, 20000, 800, 1200))
+    q = x / y
+    qb = q.view(np.uint64)
+    cases = 0
+    for k in range(len(x)):
+        for tol in (q[k], (qb[k] + np.uint64(1)).view(np.float64), (qb[k] - np.uint64(1)).view(np.float64),
+                    1e-7, 2.0 ** -23, np.nextafter(2.0 ** -23, 0.0)):
+            got = _ratio_lt(x[k], y[k], _ratio_bound(tol))
+            if got is not None:
+                cases += 1
+                assert got == bool(q[k] < tol), (x[k], y[k], tol)
+    assert cases > 100000
+    # zero dividends, and the kernels' typical relative differences near tol = 1e-7
+    assert _ratio_lt(0.0, 3.0, _ratio_bound(1e-7)) is True
+    rf = np.float64(0.731)
+    for d in np.linspace(-2e-7, 2e-7, 4001):
+        xr, yr = abs(np.float64(rf * d)), abs(rf) + 1e-30
+        assert _ratio_lt(xr, yr, _ratio_bound(1e-7)) == bool(xr / yr < 1e-7)

@@ -340,28 +340,39 @@ __global__ void __launch_bounds__(256) k_lc_early_collect(StepArgs a, uint64_t k
 
 // Ranks the candidates by (key, id) -- the sort's order -- and lists the Levi-Civita
 // ones with their sorted position and source index.  One block.
+constexpr size_t kLcRankSmem = (size_t)kLcEarlyCap * (8 + 4 + 4);
+
 __global__ void __launch_bounds__(1024) k_lc_early_rank(StepArgs a, const uint64_t *__restrict__ ckey,
                                                         const int32_t *__restrict__ cid,
                                                         const uint32_t *__restrict__ csrc, uint32_t *__restrict__ lsrc)
 {
-    __shared__ uint64_t sk[kLcEarlyCap];
-    __shared__ int32_t si[kLcEarlyCap];
+    extern __shared__ __align__(16) unsigned char rk_sm[];
+    uint64_t *sk = reinterpret_cast<uint64_t *>(rk_sm);
+    int32_t *si = reinterpret_cast<int32_t *>(rk_sm + (size_t)kLcEarlyCap * 8);
+    int32_t *sh = reinterpret_cast<int32_t *>(rk_sm + (size_t)kLcEarlyCap * 12);
     const unsigned cnt = a.ctr->lc_cand;
     if (cnt > (unsigned)kLcEarlyCap) return;
+    // halos are contiguous in the unsorted state as in the sorted one: a candidate's
+    // halo follows from its source index
     for (unsigned e = threadIdx.x; e < cnt; e += blockDim.x) {
         sk[e] = ckey[e];
         si[e] = cid[e];
+        sh[e] = seg_of(a.seg, (int64_t)csrc[e]);
     }
     __syncthreads();
     for (unsigned e = threadIdx.x; e < cnt; e += blockDim.x) {
         const uint64_t k = sk[e];
         const int32_t id = si[e];
-        unsigned rank = 0;
-        for (unsigned j = 0; j < cnt; j++) rank += (sk[j] < k || (sk[j] == k && si[j] < id)) ? 1u : 0u;
+        const int32_t h = sh[e];
+        unsigned rank = 0;   // (r, id) rank within the halo: every particle below is a candidate
+        for (unsigned j = 0; j < cnt; j++)
+            rank += (sh[j] == h && (sk[j] < k || (sk[j] == k && si[j] < id))) ? 1u : 0u;
         const uint32_t s = csrc[e];
-        if (route_lc(a, Local{(int64_t)rank, a.n, 0}, a.r_src[s], a.l_src[s])) {
+        const int64_t st = a.seg.nseg <= 1 ? 0 : a.seg.start[h];
+        const int64_t nh = a.seg.nseg <= 1 ? a.n : a.seg.start[h + 1] - st;
+        if (route_lc(a, Local{(int64_t)rank, nh, h}, a.r_src[s], a.l_src[s])) {
             const unsigned slot = atomicAdd(&a.ctr->lc_count, 1u);
-            a.lc_idx[slot] = rank;
+            a.lc_idx[slot] = (uint32_t)(st + rank);
             lsrc[slot] = s;
         }
     }
@@ -987,6 +998,8 @@ int lc_setup(nsg_ctx *c)
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_levi_civita_lanes, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_levi_civita_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_lc_early_rank, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLcRankSmem);
     if (e != cudaSuccess) return cuda_err(c, e, "levi-civita kernel setup");
     c->lc_smem = smem;
     return NSG_OK;
@@ -1082,8 +1095,8 @@ int integrate_adaptive(nsg_ctx *c)
 {
     const bool lc = ((c->p.method == NSG_METHOD_ADAPTIVE_LC || c->p.method == NSG_METHOD_FULL_LC) &&
                      c->p.lc_rule != NSG_LC_OFF);
-    // fixed-radius rule, one halo: the Levi-Civita list is made before the sort
-    const bool early = lc && c->p.lc_rule == NSG_LC_RADIUS && c->nseg == 1;
+    // fixed-radius rule: the Levi-Civita list is made before the sort
+    const bool early = lc && c->p.lc_rule == NSG_LC_RADIUS;
     if (!early)
         if (int rc = sort_perm(c)) return rc;
     StepArgs a = make_args(c);
@@ -1110,7 +1123,7 @@ int integrate_adaptive(nsg_ctx *c)
             ProfScope ps(c, "lc_prepass", (double)c->n * 8);
             k_lc_early_collect<<<grid_for(c, c->n, 256, 4), 256, 0, s>>>(a, radius_key_host(c->p.lc_radius), ckey,
                                                                           cid, csrc);
-            k_lc_early_rank<<<1, 1024, 0, s>>>(a, ckey, cid, csrc, lsrc);
+            k_lc_early_rank<<<1, 1024, kLcRankSmem, s>>>(a, ckey, cid, csrc, lsrc);
             c->launches += 2;
         }
         e = cudaEventRecord(c->ev_fork, s);

@@ -51,6 +51,35 @@ def test_ensemble_steps_equal_single_halo_runs(nsg, oracle, method):
         assert abs(K[h] - oK) <= 1e-12 * abs(oK) and abs(W[h] - oW) <= 1e-12 * abs(oW)
 
 
+@pytest.mark.parametrize("lc_radius,nmax,steps", [(0.1, 20000, 3), (0.3, 20000, 1), (1.0, 4000, 1)])
+def test_ensemble_levi_civita_list_before_the_sort(nsg, oracle, lc_radius, nmax, steps):
+    """The fixed-radius Levi-Civita list of an ensemble is made before the sort, each
+    candidate ranked within its own halo; with more candidates than the list holds
+    (lc_radius 1.0) the list made after the sort takes over.  Every halo evolves as it
+    would alone."""
+    r, vr, ell, ids, hn, start = _halos(seed=11, nhalo=6, nmin=1500, nmax=nmax)
+    r, vr, ell, ids = _shuffle_within(start, 2, r, vr, ell, ids)
+    kw = dict(dt=1e-3, max_subdiv=64, lc_rule=1, lc_radius=lc_radius, max_tau_steps=1_000_000)
+    p = oracle.params(dt=1e-3, max_subdiv=64, lc_rule=1, lc_radius=lc_radius)
+    with nsg.Context(nsg.default_params(**kw)) as c:
+        c.upload_ensemble(r, vr, ell, ids, hn)
+        c.step(steps)
+        gr, gv, gl, gid = c.download()
+        glv = c.levels()
+    n_lc = 0
+    for h in range(len(hn)):
+        a, b = start[h], start[h + 1]
+        cur = (r[a:b], vr[a:b], ell[a:b], ids[a:b] - a)
+        for _ in range(steps):
+            out = oracle.step_adaptive(p, *cur)
+            cur, olv = out[:4], out[4]
+        n_lc += int(np.sum(olv >= 99))
+        assert np.array_equal(gid[a:b] - a, cur[3]), h
+        assert np.array_equal(glv[a:b], olv), h
+        assert np.array_equal(gr[a:b], cur[0]) and np.array_equal(gv[a:b], cur[1]), h
+    assert n_lc > (4096 if lc_radius == 1.0 else 10)
+
+
 def test_ensemble_radix_fallback_and_bucket_path(nsg, oracle):
     """First sort of shuffled halos runs the radix sort with the halo passes; the
     second runs the near-sorted bucket path per halo; both give per-halo order."""

@@ -391,6 +391,7 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_lcsel, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->body, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->ctr, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMemset(c->ctr, 0, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_ctr, sizeof(DevCounters));
@@ -424,6 +425,7 @@ void nsg_destroy(nsg_ctx *c)
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->ev_lcsel) cudaEventDestroy(c->ev_lcsel);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->body) cudaStreamDestroy(c->body);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }

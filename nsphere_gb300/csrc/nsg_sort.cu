@@ -325,24 +325,16 @@ __global__ void k_finalize_energy(const double *__restrict__ kpart, const double
 }
 
 // Sorts the live copy by (halo, r, id); leaves the permutation in c->perm.
-int sort_perm(nsg_ctx *c)
+// Seed keys and the radix passes on stream s; returns the buffer that ends with the
+// permutation.  Every kernel returns at once unless ctr->need_fallback is set.
+static int launch_radix(nsg_ctx *c, cudaStream_t s, int *kb_out)
 {
     const int64_t n = c->n;
     const int src = c->cur;
     const int ntiles = (int)((n + kRadixTile - 1) / kRadixTile);
-    cudaStream_t s = c->stream;
     const Seg sg = seg_table(c);
-    // near-sorted fast path when the array is in the order of a previous sort;
-    // the radix kernels below run only if it overflowed (or it was not used)
-    if (c->split_valid && c->p.sort_mode == 0) {
-        if (int rc = bucket_sort_perm(c)) return rc;
-    } else {
-        // any non-zero value selects the radix path (bytes set to 0x01)
-        cudaError_t e = cudaMemsetAsync(&c->ctr->need_fallback, 1, sizeof(unsigned), s);
-        if (e != cudaSuccess) return cuda_err(c, e, "fallback flag");
-    }
     {
-        ProfScope ps(c, "sort_seed", (double)n * (8 + 4 + 8 + 4));
+        ProfScope ps(c, "sort_seed", (double)n * (8 + 4 + 8 + 4), s);
         k_seed_keys<<<grid_for(c, n, 256), 256, 0, s>>>(c->r[src], c->id[src], n, c->keys[0],
                                                          c->vals[0], c->ctr);
     }
@@ -352,7 +344,7 @@ int sort_perm(nsg_ctx *c)
     const int npass = 8 + (c->nseg > 1 ? 2 : 0);
     int kb = 0;
     {
-        ProfScope ps(c, "sort_radix", (double)n * npass * (8 + 12 + 12));
+        ProfScope ps(c, "sort_radix", (double)n * npass * (8 + 12 + 12), s);
         for (int pass = 0; pass < npass; pass++) {
             const int shift = pass < 8 ? pass * kRadixBits : -(pass - 8 + 1);
             k_tile_hist<<<ntiles, kRadixThreads, 0, s>>>(c->keys[kb], c->vals[kb], n, shift, ntiles,
@@ -365,10 +357,71 @@ int sort_perm(nsg_ctx *c)
             kb = 1 - kb;
         }
     }
-    c->perm = c->vals[kb];
-    c->launches += 1 + npass * 4;
-    cudaError_t e = cudaGetLastError();
+    *kb_out = kb;
+    const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "sort kernels");
+}
+
+__global__ void k_radix_cond(cudaGraphConditionalHandle h, const DevCounters *__restrict__ ctr)
+{
+    if (threadIdx.x == 0) cudaGraphSetConditional(h, ctr->need_fallback ? 1u : 0u);
+}
+
+int sort_perm(nsg_ctx *c)
+{
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    // near-sorted fast path when the array is in the order of a previous sort;
+    // the radix kernels below run only if it overflowed (or it was not used)
+    if (c->split_valid && c->p.sort_mode == 0) {
+        if (int rc = bucket_sort_perm(c)) return rc;
+    } else {
+        // any non-zero value selects the radix path (bytes set to 0x01)
+        cudaError_t e = cudaMemsetAsync(&c->ctr->need_fallback, 1, sizeof(unsigned), s);
+        if (e != cudaSuccess) return cuda_err(c, e, "fallback flag");
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr);
+    if (e != cudaSuccess) return cuda_err(c, e, "capture status");
+    int kb = 0;
+    if (cs != cudaStreamCaptureStatusActive) {
+        if (int rc = launch_radix(c, s, &kb)) return rc;
+        const int npass = 8 + (c->nseg > 1 ? 2 : 0);
+        c->launches += 1 + npass * 4;
+    } else {
+        // In a captured step the radix kernels sit in the body of a conditional node
+        // that a one-thread kernel opens only when the near-sorted path overflowed:
+        // the 33-41 launches that would return at once cost nothing.
+        cudaGraphConditionalHandle h;
+        e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+        if (e != cudaSuccess) return cuda_err(c, e, "conditional handle");
+        k_radix_cond<<<1, 32, 0, s>>>(h, c->ctr);
+        c->launches += 1;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t nd = 0;
+        e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd);
+        if (e != cudaSuccess) return cuda_err(c, e, "capture dependencies");
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp);
+        if (e != cudaSuccess) return cuda_err(c, e, "conditional node");
+        e = cudaStreamBeginCaptureToGraph(c->body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) return cuda_err(c, e, "conditional body capture");
+        const int rc = launch_radix(c, c->body, &kb);
+        cudaGraph_t bg = nullptr;
+        e = cudaStreamEndCapture(c->body, &bg);
+        if (rc) return rc;
+        if (e != cudaSuccess) return cuda_err(c, e, "conditional body capture");
+        e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e != cudaSuccess) return cuda_err(c, e, "capture dependencies");
+    }
+    c->perm = c->vals[kb];
+    return NSG_OK;
 }
 
 static int gather(nsg_ctx *c, bool kick)

@@ -44,3 +44,33 @@ def test_graph_replay_ensemble(nsg):
             out.append(c.download())
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("method", [2, 5])
+def test_graph_replay_with_radix_fallback(nsg, method):
+    """10000 particles at rest at r = 1 without gravity keep equal radii, so every
+    near-sorted sort overflows its bucket and the radix sort runs: in a replayed graph
+    it sits in a conditional node that the overflow opens.  Replay equals eager launches,
+    and the equal radii stay ordered by id."""
+    rng = np.random.default_rng(8)
+    n, ntie = 30000, 10000
+    r = rng.uniform(0.1, 3.0, n)
+    vr = rng.normal(0.0, 0.1, n)
+    ell = rng.uniform(0.0, 0.5, n)
+    tie = rng.choice(n, ntie, replace=False)
+    r[tie], vr[tie], ell[tie] = 1.0, 0.0, 0.0
+    ids = rng.permutation(n).astype(np.int32)
+    kw = dict(dt=1e-3, G=0.0, method=method, max_subdiv=64, lc_rule=2, max_tau_steps=1_000_000)
+    out = []
+    for graph in (0, 1):
+        with nsg.Context(nsg.default_params(graph=graph, **kw)) as c:
+            c.upload(r, vr, ell, ids)
+            c.step(8)
+            out.append(c.download())
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+    gr, _, _, gid = out[1]
+    at1 = gr == 1.0
+    assert at1.sum() == ntie and np.all(np.diff(gid[at1]) > 0)
+    if method == 2:   # the fixed-step body ends with the sort; the adaptive one integrates after it
+        assert np.all(np.diff(gr) >= 0)

@@ -330,7 +330,8 @@ int nsg_probe_fp64(double *dfma_tflops, double *div_hw_gps, double *div_int_gps,
 /* Dependent latencies in cycles per iteration, one block on one SM (no reference
  * counterpart): cycles[0] FP64 FMA chain; [1] two independent FMA chains in one warp;
  * [2] one chain in each of two warps; [3] dadd + FP64-pipe division; [4] dadd +
- * integer-pipe division (throughput form); [5] dadd + latency-oriented division;
+ * the throughput kernels' division (latency form, fallback behind a call); [5] dadd +
+ * latency-oriented division;
  * [6] 32-bit integer multiply-add; [7] 64-bit multiply-high; [8] int->float, multiply,
  * float->int; [9] one Levi-Civita substep of the leading warp (split force); [10] the
  * same with a zero gravity numerator; [11] the same with both force quotients in

@@ -4,13 +4,21 @@
 // GB300 runs FP64 at 1/64 of its FP32 rate, and a double division on the FP64
 // pipe costs about ten FP64 issue slots.  The integrators of the step perform
 // several divisions per force evaluation (nsphere.c:513, :535, :575, :599), so
-// division throughput bounds the step.  This routine returns the same bits as
+// division throughput bounds the step.  The routines here return the same bits as
 // IEEE division (the CPU reference's `/`) for every pair of finite normal operands
 // whose quotient is a finite normal number; all other operands (zero, subnormal,
 // infinite, NaN, quotient out of the normal range) go to the hardware division.
 //
-// Method (a textbook Newton-Raphson reciprocal in fixed point, then an exactly
-// verified quotient):
+// Two forms:
+//   div_rn_lat  three quotient digits from an FP32 reciprocal with exact integer
+//               remainders (below).  Few, short steps: the serial chains use it,
+//               and so do the throughput kernels (div_rn), once its fallback sits
+//               behind a call;
+//   div_rn_fast a Newton-Raphson reciprocal in fixed point, then an exactly
+//               verified quotient; the division self-test cross-checks it against
+//               the hardware and the latency form.
+//
+// div_rn_fast (a textbook method):
 //   mantissas ma, mb in [2^52, 2^53); A = ma or 2 ma so that A/mb lies in [1, 2);
 //   R ~ 2^105/mb: single-precision reciprocal estimate (rel. error < 2^-21),
 //       then two Newton steps R += R (2^105 - mb R) / 2^105 in 64/128-bit integers;
@@ -286,12 +294,20 @@ NSG_HD double div_rn_lat(double a, double b, bool &ok)
 }
 
 #if defined(__CUDACC__)
-// Correctly rounded a / b (round to nearest even), bit-identical to __ddiv_rn.
+// The FP64 pipe's division behind a call: the compiler cannot predicate or hoist the
+// division's instructions into the caller, so they run only for the operands the
+// integer forms leave (a predicated inline fallback halves the throughput).
+static __device__ __noinline__ double div_rn_slow(double a, double b) { return __ddiv_rn(a, b); }
+
+// Correctly rounded a / b (round to nearest even), bit-identical to __ddiv_rn: the
+// latency form, whose few integer and FP32 steps also give the highest throughput
+// once its fallback sits behind a call (248 G/s alone against 110 for div_rn_fast).
 __device__ __forceinline__ double div_rn(double a, double b)
 {
-    double q;
-    if (div_rn_fast(a, b, &q)) return q;
-    return __ddiv_rn(a, b);
+    bool ok;
+    double q = div_rn_lat(a, b, ok);
+    if (!ok) q = div_rn_slow(a, b);
+    return q;
 }
 
 // The FP64 pipe's division with the +-0 / normal case answered directly (IEEE:

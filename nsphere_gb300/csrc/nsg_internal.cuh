@@ -250,10 +250,11 @@ __device__ __forceinline__ double u32_to_double(uint32_t x)
     return __longlong_as_double((long long)((((unsigned long long)(1023 + e)) << 52) | m));
 }
 
-// Division: throughput-bound kernels divide on the integer/FP32 pipes
-// (div_rn, nsg_div.cuh); the Levi-Civita chains use the latency-oriented
-// div_rn_lat with the FP64 pipe's division as its fallback.  All are IEEE
-// round-to-nearest, so the choice never changes a result bit.
+// Division: throughput-bound kernels divide on the integer/FP32 pipes (div_rn:
+// the latency form with the FP64 pipe's division behind a call, nsg_div.cuh); the
+// Levi-Civita chains use div_rn_lat directly and redo a tau-step on the FP64 pipe
+// when it declines an operand.  All are IEEE round-to-nearest, so the choice never
+// changes a result bit.
 template <bool HW>
 __device__ __forceinline__ double ddivx(double a, double b) { return HW ? div_rn_hw(a, b) : div_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return div_rn(a, b); }

@@ -18,7 +18,8 @@
 //   k_levels_lanes   particles that failed level 0: a group of lanes per
 //                    particle, lane j computing the fine pass of level j+1 at the
 //                    same time; the group stops at the first level that agrees
-//                    with the level below (latency-bound; FP64-pipe divisions).
+//                    with the level below (latency-bound; the latency-form
+//                    division, two per force in one lane without FP64 issue slots).
 // Adaptive Levi-Civita (nsphere.c:1990-2334): one warp per particle, started on a
 // side stream right after the sort, overlapped with the leapfrog work.  Within a
 // tau-step the lanes compute the coarse N=1 pass, the fine pass of every level and
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
             const double ell = a.ell_out[i];
             l2 = dmul(ell, ell);
             const Local L = local_of(a.seg, i, a.n);
-            gn = gnum_of<true>(L.i, L.n, a.G, a.M, Mpt);
+            gn = gnum_of(L.i, L.n, a.G, a.M, Mpt);
             af = a.a0[i];
             rq = a.q_r[e];
             vq = a.q_v[e];
@@ -264,8 +265,8 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
             // one drift-kick pair; the last pair of a pass ends with the half-kick
             if (active && it < pairs) {
                 r = dadd(r, dmul(ms, v));
-                if (it + 1 < pairs) v = dadd(v, dmul(ms, acc_leap<true>(r, gn, l2)));
-                else { v = dadd(v, dmul(hk, acc_leap<true>(r, gn, l2))); rf = r; vf = v; }
+                if (it + 1 < pairs) v = dadd(v, dmul(ms, acc_leap(r, gn, l2)));
+                else { v = dadd(v, dmul(hk, acc_leap(r, gn, l2))); rf = r; vf = v; }
             }
             it++;
             // the fine pass of level kcheck ended at it = 2^(kcheck+1)
@@ -279,7 +280,7 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
                 const double rC = (!FULL && kcheck == 1) ? rq : rC0;
                 const double vC = (!FULL && kcheck == 1) ? vq : vC0;
                 if (active && kcheck >= kstart) {
-                    const bool ok = converged<true>(rC, vC, rF, vF, rF, a);
+                    const bool ok = converged<false>(rC, vC, rF, vF, rF, a);
                     const bool bad = !(finite_bits(rF) && finite_bits(vF));
                     if (ok || (bad && a.nf_stop) || kcheck == nl) {
                         if (j == 0) {

@@ -37,8 +37,8 @@ UNIT = "particle-steps/s"
 # write them 28, write the rank force 8
 SORT_PASS_BYTES = 72.0
 # DRAM bytes per particle of one k_gather_level0 launch (read + write), from an ncu capture
-# of that kernel at N = 5e6 (160.6 MB read + 122.2 MB written per launch)
-GATHER_LEVEL0_TRAFFIC = (160.628224e6 + 122.180864e6) / 5e6
+# of that kernel at N = 5e6 (160.7 MB read + 121.8 MB written per launch)
+GATHER_LEVEL0_TRAFFIC = (160.67328e6 + 121.77024e6) / 5e6
 # DRAM bytes of one k_levi_civita_pair launch, from an ncu capture of the Hernquist step
 # at N = 2e6 (62.7 KB read, nothing written back to DRAM during the launch); it does not
 # grow with N -- the launch touches only the Levi-Civita particles
@@ -466,7 +466,7 @@ def main():
                     "unit": "GB/s", "frac": ach / hbm_peak, "traffic": GATHER_LEVEL0_TRAFFIC * n,
                     "peak_source": peak_src,
                     "note": "the largest kernel beside the chains; compute-bound on the FP64 pipe "
-                            "(ncu: 75% FP64 pipe active); FP64 view below",
+                            "(ncu: 82% FP64 pipe active); FP64 view below",
                     "fp64": {"achieved_tflops": flops, "peak_tflops": fp64["dfma_tflops"],
                              "frac": flops / fp64["dfma_tflops"],
                              "peak_source": "measured live by nsg_probe_fp64 (FMA = 2 flops)"}}

@@ -551,14 +551,28 @@ static int upload_host(nsg_ctx *c, const double *r, const double *vr, const doub
     if (int rc = upload_common(c, n, seg_n, nseg)) return rc;
     const size_t b = (size_t)n * 8;
     cudaStream_t s = c->stream;
-    cudaError_t e = cudaMemcpyAsync(c->r[0], r, b, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(c->vr[0], vr, b, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(c->ell[0], ell, b, cudaMemcpyHostToDevice, s);
+    // The columns travel on three streams at once (one copy alone does not fill the
+    // host link): the ids on the main stream, whose conversion starts as soon as they
+    // arrive; r and ell on the side stream, v_r (and aux) on the third.  The main
+    // stream waits for all of them before the ids are validated, and the validation's
+    // synchronisation returns only after every copy has finished, so the caller's
+    // host arrays are free again on return, as with one stream.
+    cudaError_t e = cudaEventRecord(c->ev_fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->body, c->ev_fork, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->stage_d, id_as_double, b, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && c->p.carry_aux) e = cudaMemcpyAsync(c->aux[0], aux, b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->r[0], r, b, cudaMemcpyHostToDevice, c->side);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->vr[0], vr, b, cudaMemcpyHostToDevice, c->body);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->ell[0], ell, b, cudaMemcpyHostToDevice, c->side);
+    if (e == cudaSuccess && c->p.carry_aux) e = cudaMemcpyAsync(c->aux[0], aux, b, cudaMemcpyHostToDevice, c->body);
     if (e == cudaSuccess) e = cudaMemsetAsync(&c->ctr->pad, 0, 4, s);
     if (e != cudaSuccess) return cuda_err(c, e, "upload copy");
     k_ids_from_double<<<grid_for(c, n, 256), 256, 0, s>>>(c->stage_d, c->id[0], n, &c->ctr->pad);
+    e = cudaEventRecord(c->ev_join, c->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_join, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->body);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_join, 0);
+    if (e != cudaSuccess) return cuda_err(c, e, "upload join");
     return validate_ids(c, c->id[0], n, 0);
 }
 

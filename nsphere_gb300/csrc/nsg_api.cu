@@ -360,6 +360,28 @@ int nsg_params_default(nsg_params *p)
     return NSG_OK;
 }
 
+// Whether the driver builds an IF conditional graph node (CUDA 12.4 and later): tried
+// once on an empty graph; without it, captured steps launch the radix fallback's
+// kernels directly, as eager steps do.
+static bool cond_nodes_supported()
+{
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) { cudaGetLastError(); return false; }
+    cudaGraphConditionalHandle h;
+    bool ok = cudaGraphConditionalHandleCreate(&h, g, 0, 0) == cudaSuccess;
+    if (ok) {
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
+    }
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return ok;
+}
+
 int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
 {
     if (!out) return set_err(nullptr, NSG_EINVAL, "null ctx pointer");
@@ -392,6 +414,7 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_lcsel, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->body, cudaStreamNonBlocking);
+    if (e == cudaSuccess) c->cond_nodes = cond_nodes_supported();
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->ctr, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMemset(c->ctr, 0, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_ctr, sizeof(DevCounters));

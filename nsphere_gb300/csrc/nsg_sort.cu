@@ -385,7 +385,7 @@ int sort_perm(nsg_ctx *c)
     cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr);
     if (e != cudaSuccess) return cuda_err(c, e, "capture status");
     int kb = 0;
-    if (cs != cudaStreamCaptureStatusActive) {
+    if (cs != cudaStreamCaptureStatusActive || !c->cond_nodes) {
         if (int rc = launch_radix(c, s, &kb)) return rc;
         const int npass = 8 + (c->nseg > 1 ? 2 : 0);
         c->launches += 1 + npass * 4;

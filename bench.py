@@ -3,10 +3,17 @@
 Workload (default): N = 1e7 equal-mass Hernquist halo (a = 1, truncated at r = 100,
 isotropic distribution function, seed 2), G = M = 1, adaptive leapfrog with at most
 8 refinement levels (max_subdiv = 128), adaptive Levi-Civita below r = 1e-3,
-tolerance 1e-7, Richardson output, dt = 5e-4.  One step = radial sort + rank
-enclosed mass / force + adaptive integration of every particle.  Metric:
-particle-steps/s.  The state (28 B/particle plus sort buffers) is far larger than
-the 129 MB L2, so no flush is needed between steps.
+tolerance 1e-7, Richardson output, dt = 4e-5: the step at which |dE/E| stays below
+1e-6 over 1000 steps (the drift grows linearly in steps and as dt^2: 9.9e-5 at
+dt = 5e-4, 3.9e-6 at 1e-4, 6.3e-7 at 4e-5 over 1000 steps of this halo).  One
+step = radial sort + rank enclosed mass / force + adaptive integration of every
+particle.  Metric: particle-steps/s.  The state (28 B/particle plus sort buffers)
+is far larger than the 129 MB L2, so no flush is needed between steps.
+
+Besides the timed region, both level schedules run 1000 steps from the same start
+state (|dE/E| over those 1000 steps and their rate): the learned one after its
+network is trained on levels logged from 200 plain steps of the N = 1e7 Hernquist
+halo.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -51,14 +58,17 @@ LEVEL0_FLOPS = 46.0
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=10_000_000)
     ap.add_argument("--workload", choices=["adaptive", "kdk", "ensemble", "om", "stress"], default="adaptive")
     ap.add_argument("--sched", choices=["plain", "learned"], default="plain")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--ab-steps", type=int, default=8, help="steps of the learned/plain comparison (0: skip)")
+    ap.add_argument("--ab-steps", type=int, default=1000,
+                    help="steps of each schedule in the learned/plain comparison and drift run (0: skip)")
+    ap.add_argument("--train-steps", type=int, default=200, help="plain steps whose levels train the scheduler")
+    ap.add_argument("--dt", type=float, default=None, help="time step (default: the workload's)")
     ap.add_argument("--nonfinite-stop", type=int, default=1, help="stress workload: 0 follows the reference on non-finite passes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--post-runs", type=int, default=3,
@@ -67,9 +77,15 @@ def parse():
     return ap.parse_args()
 
 
+# time step of the adaptive workloads: |dE/E| <= 1e-6 over 1000 steps of the N = 1e7
+# Hernquist halo (6.3e-7 measured; 9.8e-7 at 5e-5, 3.9e-6 at 1e-4, 9.9e-5 at 5e-4)
+DT_EQUAL_DRIFT = 4e-5
+
+
 def workload(args, seed_offset=0):
     from nsphere_gb300.replicas import replica_seed
     from nsphere_gb300 import ics
+    dt_eq = DT_EQUAL_DRIFT
     if args.workload == "kdk":
         cfg = dict(workload="plummer_kdk_fixed_step", n=args.n, profile="plummer", seed=replica_seed(1, seed_offset),
                    dt=1e-3, method="fixed-step leapfrog (reference method 2)")
@@ -85,7 +101,7 @@ def workload(args, seed_offset=0):
         args.n = int(len(r))
     elif args.workload == "om":
         cfg = dict(workload="hernquist_om_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 osipkov-merritt r_a=1",
-                   seed=replica_seed(4, seed_offset), dt=5e-4, max_levels=8, max_subdiv=128,
+                   seed=replica_seed(4, seed_offset), dt=dt_eq, max_levels=8, max_subdiv=128,
                    lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
         # generated on the GPU (nsg_generate_om, closed-form Osipkov-Merritt f(Q))
         import nsphere_gb300 as ns
@@ -93,7 +109,7 @@ def workload(args, seed_offset=0):
             g.generate_om(args.n, replica_seed(4, seed_offset), 100.0, 1.0)
             state = g.download()
         cfg["generator"] = "nsg_generate_om"
-        params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
+        params = dict(dt=dt_eq, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
     elif args.workload == "stress":
         # Hernquist, 20 % of the particles on near-radial orbits (ell uniform in [0, 1e-4]),
         # a central point mass ramped from 0 to 0.01 over 500 steps
@@ -116,10 +132,15 @@ def workload(args, seed_offset=0):
                       point_mass_rate=0.01 / (500 * 5e-4), nonfinite_stop=args.nonfinite_stop)
     else:
         cfg = dict(workload="hernquist_adaptive_lc", n=args.n, profile="hernquist a=1 r<=100 isotropic",
-                   seed=replica_seed(2, seed_offset), dt=5e-4, max_levels=8, max_subdiv=128,
+                   seed=replica_seed(2, seed_offset), dt=dt_eq, max_levels=8, max_subdiv=128,
                    lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
         state = ics.hernquist(args.n, seed=replica_seed(2, seed_offset))
-        params = dict(dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
+        params = dict(dt=dt_eq, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
+    if args.dt is not None:
+        # an explicit time step replaces the workload's (the point-mass ramp keeps its 500 steps)
+        if "point_mass_rate" in params:
+            params["point_mass_rate"] = 0.01 / (500 * args.dt)
+        params["dt"] = cfg["dt"] = args.dt
     cfg["l2"] = "inputs larger than L2 (state %.0f MB vs 129 MB L2); no flush" % (args.n * 28 / 1e6)
     cfg["sched"] = args.sched
     return cfg, state, params
@@ -169,8 +190,10 @@ class Clocks:
                 "reasons": reasons, "samples": len(sm)}
 
 
-def cpu_stepper(params):
-    """The reference's own step functions (oracle/_ref, all host threads), else the port."""
+def cpu_stepper(params, parallel_sort=True):
+    """The reference's own step functions (oracle/_ref, all host threads), else the port.
+    parallel_sort: the reference's default quadsort_parallel (True) or its exact
+    sequential quadsort (False)."""
     from oracle import build_oracle
     from oracle.oracle import Oracle, Reference
     try:
@@ -181,11 +204,11 @@ def cpu_stepper(params):
 
         def step(cur):
             if params.get("method") == 2:
-                tab, _ = R.step_kdk(cur[0], cur[1], cur[2], cur[3], params["dt"], parallel_sort=True)
+                tab, _ = R.step_kdk(cur[0], cur[1], cur[2], cur[3], params["dt"], parallel_sort=parallel_sort)
             else:
                 tab, _ = R.step_method5(cur[0], cur[1], cur[2], cur[3], params["dt"],
                                         max_subdiv=params["max_subdiv"], lc_rule=params["lc_rule"],
-                                        lc_radius=params["lc_radius"], parallel_sort=True)
+                                        lc_radius=params["lc_radius"], parallel_sort=parallel_sort)
             return tab[0], tab[1], tab[2], tab[3]
     except (FileNotFoundError, RuntimeError, OSError):
         build_oracle.build_oracle()
@@ -206,21 +229,30 @@ def cpu_stepper(params):
 
 
 def cpu_baseline(state, params, seconds):
-    """Reference CPU step on the full N-particle state, repeated for about `seconds`."""
-    step, cores, kind = cpu_stepper(params)
+    """Reference CPU step on the full N-particle state, repeated for about `seconds`
+    with its default parallel sort, then for about a third of that with its exact
+    sequential quadsort."""
+    from oracle import build_oracle
     r, vr, ell, ids = state
     n = len(r)
-    cur = (r, vr, ell, ids.astype(np.float64))
-    steps, elapsed = 0, 0.0
-    while (elapsed < seconds or steps == 0) and steps < 1000:
-        t0 = time.perf_counter()
-        cur = step(cur)
-        elapsed += time.perf_counter() - t0
-        steps += 1
-    flags = "gcc -O2 -ffast-math -fopenmp" if kind == "reference" else "gcc -O2 -fopenmp"
-    return {"value": n * steps / elapsed, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": "%d full steps of the N=%d state (%.1f s of CPU work; default quadsort_parallel; %s)"
-                      % (steps, n, elapsed, flags)}
+    out = {}
+    for par, budget in ((True, seconds), (False, seconds / 3)):
+        step, cores, kind = cpu_stepper(params, parallel_sort=par)
+        cur = (r, vr, ell, ids.astype(np.float64))
+        steps, elapsed = 0, 0.0
+        while (elapsed < budget or steps == 0) and steps < 1000:
+            t0 = time.perf_counter()
+            cur = step(cur)
+            elapsed += time.perf_counter() - t0
+            steps += 1
+        out[par] = (n * steps / elapsed, steps, elapsed, cores, kind)
+    value, steps, elapsed, cores, kind = out[True]
+    flags = build_oracle.fast_flags_used() if kind == "reference" else "gcc -O2 -fopenmp (oracle port)"
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+            "value_exact_quadsort": out[False][0],
+            "sample": "%d full steps of the N=%d state (%.1f s of CPU work) with the default quadsort_parallel; "
+                      "%d steps (%.1f s) with the exact sequential quadsort (value_exact_quadsort); built with: %s"
+                      % (steps, n, elapsed, out[False][1], out[False][2], flags)}
 
 
 def run_reference_arm(args, rank, world):
@@ -352,39 +384,72 @@ def main():
     ctx.profile(False)
     ctx.set_params(p)
 
-    # learned against plain schedule on the same state: collect levels from plain steps,
-    # train on the GPU, then time the same steps under each schedule from one snapshot.
-    # Both schedules give bit-identical states, so |dE/E| is equal by construction.
+    # learned against plain schedule, and the energy drift of each over 1000 steps.
+    # Training set: the accepted levels of `train_steps` plain steps of the N = 1e7
+    # Hernquist halo (the default workload), collected and trained on the GPU.  Then
+    # each schedule runs `ab_steps` steps from the workload's start state; both give
+    # bit-identical states (the plain error test judges every particle), so their
+    # |dE/E| are equal by construction and measured here over the whole run.
     learned = None
-    if args.workload in ("adaptive", "om") and args.ab_steps > 0:
+    if args.workload in ("adaptive", "om") and args.ab_steps > 0 and sizes is None:
+        ctx.set_params(ns.default_params(**params))
+        if args.workload == "adaptive":
+            ctx.upload(r, vr, ell, ids)
+        else:
+            ctx.generate(ns.IC_HERNQUIST, n, 2, 100.0)
         ctx.mlp_init(4)
-        ctx.mlp_collect(3, keep_level0=0.02, capacity=1 << 21)
+        # level 0 holds all but ~1e-5 of the particles at this dt: keep 1e-4 of them
+        ctx.mlp_collect(args.train_steps, keep_level0=1e-4, capacity=1 << 21)
+        _, ytrain = ctx.mlp_dataset()
         loss = ctx.mlp_train(epochs=4, batch=2048, lr=3e-3, seed=4)
-        snap = ctx.download()
+        warm = 3
 
-        def timed(sched):
+        def run_schedule(sched):
             q = ns.default_params(**params)
             q.sched = sched
             ctx.set_params(q)
-            ctx.upload(*snap)
-            ctx.step(1)
+            ctx.upload(r, vr, ell, ids)
+            e_start = sum(ctx.energy())
+            ctx.step(warm)
             barrier()
             t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             t0.record(stream)
-            ctx.step(args.ab_steps)
+            ctx.step(args.ab_steps - warm)
             t1.record(stream)
             barrier()
-            return t0.elapsed_time(t1), sum(ctx.energy()), ctx.download()
+            ms_ = t0.elapsed_time(t1)
+            e_end = sum(ctx.energy())
+            final = ctx.download()
+            lv = ctx.level_hist(10)
+            # the kernels beside the Levi-Civita chains, per step, over 20 further steps
+            ctx.profile(True)
+            ctx.step(20)
+            pr = ctx.profile_read()
+            ctx.profile(False)
+            bulk_ms = sum(k["total_ms"] for k in pr if k["name"] not in ("levi_civita", "lc_late")) / 20
+            return {"value": n * (args.ab_steps - warm) / (ms_ / 1e3), "ms_per_step": ms_ / (args.ab_steps - warm),
+                    "dE_over_E": abs(e_end - e_start) / abs(e_start), "steps": args.ab_steps,
+                    "timed_steps": args.ab_steps - warm, "bulk_ms_per_step": bulk_ms,
+                    "level_hist_last_step": [int(x) for x in lv],
+                    "kernels": {k["name"]: k["total_ms"] / 20 for k in pr}}, final
 
-        ms_l, e_l, s_l = timed(ns.SCHED_LEARNED)
-        ms_p, e_p, s_p = timed(ns.SCHED_PLAIN)
+        res_p, s_p = run_schedule(ns.SCHED_PLAIN)
+        res_l, s_l = run_schedule(ns.SCHED_LEARNED)
         same = all(np.array_equal(a_, b_) for a_, b_ in zip(s_l, s_p))
-        learned = {"steps": args.ab_steps, "train_loss": loss,
-                   "learned_value": n * args.ab_steps / (ms_l / 1e3),
-                   "plain_value": n * args.ab_steps / (ms_p / 1e3),
-                   "speedup": ms_p / ms_l, "identical_states": bool(same),
-                   "dE_over_E_learned": abs(e_l - E0) / abs(E0), "dE_over_E_plain": abs(e_p - E0) / abs(E0)}
+        del s_l, s_p
+        learned = {"train_steps": args.train_steps, "train_halo": "hernquist a=1 r<=100 isotropic, N=%d" % n,
+                   "train_samples": int(len(ytrain)),
+                   "train_class_counts": [int(x) for x in np.bincount(ytrain.astype(np.int64), minlength=8)],
+                   "train_loss": loss, "plain": res_p, "learned": res_l,
+                   "learned_value": res_l["value"], "plain_value": res_p["value"],
+                   "speedup": res_l["value"] / res_p["value"],
+                   "bulk_speedup": res_p["bulk_ms_per_step"] / res_l["bulk_ms_per_step"],
+                   "identical_states": bool(same),
+                   "dE_over_E_learned": res_l["dE_over_E"], "dE_over_E_plain": res_p["dE_over_E"],
+                   "energy_drift_steps": args.ab_steps}
+        del ytrain
         ctx.set_params(p)
+        ctx.upload(r, vr, ell, ids)
 
     # end to end through the public C ABI with host buffers: upload (pinned), step, download
     pin = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(8)]
@@ -529,8 +594,12 @@ def main():
             "kernels": [{"name": k["name"], "ms_per_step": k["total_ms"] / nprof, "share": k["total_ms"] / tot}
                         for k in prof],
             "fp64_probe": fp64,
-            "energy_drift": abs(E1 - E0) / abs(E0),
-            "energy_drift_steps": args.warmup + args.steps,
+            # |dE/E| over 1000 steps of each schedule (the learned/plain runs), else over the
+            # warm-up and timed steps
+            "energy_drift": learned["dE_over_E_plain"] if learned else abs(E1 - E0) / abs(E0),
+            "energy_drift_steps": learned["energy_drift_steps"] if learned else args.warmup + args.steps,
+            "energy_drift_learned": learned["dE_over_E_learned"] if learned else None,
+            "energy_drift_timed_region": abs(E1 - E0) / abs(E0),
             "level_hist": [int(x) for x in hist],
             "status": status,
             "learned_vs_plain": learned,

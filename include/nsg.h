@@ -177,9 +177,12 @@ int nsg_sort_particles(nsg_ctx *ctx, double *const *particles, int64_t npts);
  * ties by id, then input position -- with no context and no device allocation,
  * its scratch being one fixed 34,078,720-byte __device__ array per device.
  * npts > 1048576 returns NSG_EINVAL untouched; aux may be NULL; work is queued
- * on `stream` (a cudaStream_t of the current device, NULL = legacy default).  The
- * first call on a device looks the scratch address up (cudaGetSymbolAddress) and
- * should come before any stream capture.  Calls that overlap in time on one
+ * on `stream` (a cudaStream_t of the current device, NULL = legacy default).  A call
+ * outside stream capture looks the scratch address up (cudaGetSymbolAddress), so it
+ * follows a device reset or a new context; a call made while `stream` is being
+ * captured reuses the address of the last call on the device, so the first call on a
+ * device should come before any capture.  A CUDA error pending from earlier work is
+ * returned (NSG_ECUDA) without running the sort.  Calls that overlap in time on one
  * device share the scratch and race: keep them on one stream. */
 int nsg_sort_device_noalloc(double *d_r, double *d_vr, double *d_ell, int32_t *d_id, double *d_aux,
                             int64_t npts, void *stream);

@@ -285,19 +285,39 @@ static int ensure_capacity(nsg_ctx *c, int64_t n)
     const size_t d8 = (size_t)n * 8, d4 = (size_t)n * 4;
     const int64_t ntiles = (n + kRadixTile - 1) / kRadixTile;
     cudaError_t e = cudaSuccess;
+    // two passes over the same list: the first only adds the sizes up, so that a
+    // state that cannot fit is refused before anything is allocated
+    bool count_only = true;
+    size_t need = 0;
     auto A = [&](auto *&p, size_t bytes) {
-        if (e == cudaSuccess) e = cudaMalloc((void **)&p, bytes ? bytes : 16);
+        bytes = bytes ? bytes : 16;
+        if (count_only) { need += (bytes + 511) & ~(size_t)511; return; }
+        if (e == cudaSuccess) e = cudaMalloc((void **)&p, bytes);
     };
-    for (int b = 0; b < 2; b++) {
-        A(c->r[b], d8); A(c->vr[b], d8); A(c->ell[b], d8); A(c->id[b], d4);
-        if (c->p.carry_aux) A(c->aux[b], d8);
-        A(c->keys[b], d8); A(c->vals[b], d4);
-        A(c->q_idx[b], d4); A(c->q_r[b], d8); A(c->q_v[b], d8);
+    auto all = [&]() {
+        for (int b = 0; b < 2; b++) {
+            A(c->r[b], d8); A(c->vr[b], d8); A(c->ell[b], d8); A(c->id[b], d4);
+            if (c->p.carry_aux) A(c->aux[b], d8);
+            A(c->keys[b], d8); A(c->vals[b], d4);
+            A(c->q_idx[b], d4); A(c->q_r[b], d8); A(c->q_v[b], d8);
+        }
+        A(c->a0, d8); A(c->inv, d4); A(c->level, (size_t)n);
+        A(c->tile_counts, (size_t)ntiles * kRadixBuckets * 4); A(c->digit_tot, kRadixBuckets * 4);
+        A(c->lc_idx, d4); A(c->red_part, 2 * kReduceBlocks * 8); A(c->stage_d, d8);
+        A(c->lc_early, (size_t)kLcEarlyCap * 20);
+    };
+    all();
+    size_t free_b = 0, total_b = 0;
+    e = cudaMemGetInfo(&free_b, &total_b);
+    if (e != cudaSuccess) return cuda_err(c, e, "device memory query");
+    if (need > free_b) {
+        char msg[160];
+        snprintf(msg, sizeof msg, "device allocation: %lld particles need %.1f GB of device buffers, %.1f GB free",
+                 (long long)n, need / 1e9, free_b / 1e9);
+        return set_err(c, NSG_ENOMEM, msg);
     }
-    A(c->a0, d8); A(c->inv, d4); A(c->level, (size_t)n);
-    A(c->tile_counts, (size_t)ntiles * kRadixBuckets * 4); A(c->digit_tot, kRadixBuckets * 4);
-    A(c->lc_idx, d4); A(c->red_part, 2 * kReduceBlocks * 8); A(c->stage_d, d8);
-    A(c->lc_early, (size_t)kLcEarlyCap * 20);
+    count_only = false;
+    all();
     if (e != cudaSuccess) {
         free_buffers(c);
         return cuda_err(c, e, "device allocation");
@@ -589,13 +609,27 @@ static int upload_host(nsg_ctx *c, const double *r, const double *vr, const doub
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->ell[0], ell, b, cudaMemcpyHostToDevice, c->side);
     if (e == cudaSuccess && c->p.carry_aux) e = cudaMemcpyAsync(c->aux[0], aux, b, cudaMemcpyHostToDevice, c->body);
     if (e == cudaSuccess) e = cudaMemsetAsync(&c->ctr->pad, 0, 4, s);
-    if (e != cudaSuccess) return cuda_err(c, e, "upload copy");
+    if (e != cudaSuccess) {
+        // copies already queued may still read the caller's arrays: wait for them, so
+        // the arrays are free on every return, and leave no unjoined work behind
+        const int rc = cuda_err(c, e, "upload copy");
+        cudaStreamSynchronize(c->side);
+        cudaStreamSynchronize(c->body);
+        cudaStreamSynchronize(s);
+        return rc;
+    }
     k_ids_from_double<<<grid_for(c, n, 256), 256, 0, s>>>(c->stage_d, c->id[0], n, &c->ctr->pad);
     e = cudaEventRecord(c->ev_join, c->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_join, 0);
     if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->body);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_join, 0);
-    if (e != cudaSuccess) return cuda_err(c, e, "upload join");
+    if (e != cudaSuccess) {
+        const int rc = cuda_err(c, e, "upload join");
+        cudaStreamSynchronize(c->side);
+        cudaStreamSynchronize(c->body);
+        cudaStreamSynchronize(s);
+        return rc;
+    }
     return validate_ids(c, c->id[0], n, 0);
 }
 

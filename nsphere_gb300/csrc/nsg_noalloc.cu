@@ -190,16 +190,23 @@ __global__ void k_na_gather_id(const int32_t *__restrict__ id, const uint64_t *_
     out[i] = id[uint32_t(tag[i])];
 }
 
-// Address of the scratch array on the current device (looked up once per device).
-int na_scratch(unsigned char **out)
+// Address of the scratch array on the current device.  Outside stream capture it is
+// looked up on every call (cheap once the module is loaded), so a context that was
+// reset or replaced since the last call -- the array may then sit at a new address --
+// is followed; calls made while `s` is being captured use the address cached by the
+// last call on this device, which must therefore come before the capture.
+int na_scratch(cudaStream_t s, unsigned char **out)
 {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_err(nullptr, e, "nsg_sort_device_noalloc: no current device");
     if (dev < 0 || dev >= kNaMaxDevices)
         return set_err(nullptr, NSG_EDEVICE, "nsg_sort_device_noalloc: device ordinal out of range");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess) return cuda_err(nullptr, e, "nsg_sort_device_noalloc: stream query");
     std::lock_guard<std::mutex> lock(g_na_mu);
-    if (!g_na_base[dev]) {
+    if (cap == cudaStreamCaptureStatusNone || !g_na_base[dev]) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_na_scratch);
         if (e != cudaSuccess) return cuda_err(nullptr, e, "nsg_sort_device_noalloc: scratch address lookup");
@@ -222,9 +229,12 @@ extern "C" int nsg_sort_device_noalloc(double *d_r, double *d_vr, double *d_ell,
     if (n > 0 && (!d_r || !d_vr || !d_ell || !d_id))
         return set_err(nullptr, NSG_EINVAL, "nsg_sort_device_noalloc: null column");
     if (n <= 1) return NSG_OK;
-    unsigned char *base = nullptr;
-    if (int rc = na_scratch(&base)) return rc;
+    // an error left by earlier work of the caller is reported as such, not as this sort's
+    cudaError_t pre = cudaGetLastError();
+    if (pre != cudaSuccess) return cuda_err(nullptr, pre, "nsg_sort_device_noalloc: CUDA error pending before the call");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned char *base = nullptr;
+    if (int rc = na_scratch(s, &base)) return rc;
     const int m = int(n);
     const int ntiles = (m + kNaTile - 1) / kNaTile;
     const int blocks = (m + 255) / 256;
@@ -242,6 +252,10 @@ extern "C" int nsg_sort_device_noalloc(double *d_r, double *d_vr, double *d_ell,
         k_na_scatter<<<ntiles, kNaThreads, 0, s>>>(key[a], tag[a], key[a ^ 1], tag[a ^ 1], m, pass, ntiles,
                                                    count);
     }
+    // a failed launch of the sort passes leaves the caller's columns untouched: the
+    // gathers and copies below, which overwrite them, are not queued
+    cudaError_t le = cudaPeekAtLastError();
+    if (le != cudaSuccess) return cuda_err(nullptr, cudaGetLastError(), "nsg_sort_device_noalloc: sort kernels");
     // the sorted tags are in tag[0] (even pass count); key[1] and tag[1] are free
     double *t0 = reinterpret_cast<double *>(key[1]);
     double *t1 = reinterpret_cast<double *>(tag[1]);

@@ -1,6 +1,8 @@
 """nsg_sort_device_noalloc, the allocation-free sort of caller-owned device columns,
-against the context sort nsg_sort_particles on the same inputs.  The file name makes
-it collect last, so that it runs both alone and after every other test."""
+against the context sort nsg_sort_particles and the oracle on the same inputs, and
+with the device's free memory and torch's allocation counters unchanged by a call.
+The file name makes it collect last, so that it runs both alone and after every
+other test."""
 import ctypes as C
 
 import numpy as np
@@ -59,7 +61,7 @@ def test_rejects_bad_sizes_without_device_work(nsg):
 
 
 @pytest.mark.gpu
-def test_two_calls_in_a_row_match_context_sort(nsg):
+def test_two_calls_in_a_row_match_context_sort(nsg, oracle):
     torch = pytest.importorskip("torch")
     a = _inputs(300_001, seed=71)                  # ragged last tile, with aux
     b = _inputs(77_777, seed=72)[:4] + (None,)     # aux NULL
@@ -76,6 +78,28 @@ def test_two_calls_in_a_row_match_context_sort(nsg):
         assert _same(got.cpu().numpy(), want)
     for got, want in zip(dev_b, want_b):
         assert _same(got.cpu().numpy(), want)
+    # and directly against the oracle's (r, id) sort
+    for got, want in zip(dev_a, oracle.sort(*a)):
+        assert _same(got.cpu().numpy(), want)
+    for got, want in zip(dev_b, oracle.sort(*b[:4])):
+        assert _same(got.cpu().numpy(), want)
+
+
+@pytest.mark.gpu
+def test_a_call_allocates_no_device_memory(nsg):
+    torch = pytest.importorskip("torch")
+    cols = _inputs(MAX_N, seed=76)
+    dev = _device(torch, cols)
+    stream = torch.cuda.current_stream().cuda_stream
+    torch.cuda.synchronize()
+    assert _call(nsg, dev, MAX_N, stream) == nsg.NSG_OK      # warm: module and scratch loaded
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    allocs0 = torch.cuda.memory_stats().get("allocation.all.allocated", 0)
+    assert _call(nsg, dev, MAX_N, stream) == nsg.NSG_OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_stats().get("allocation.all.allocated", 0) == allocs0
 
 
 @pytest.mark.gpu

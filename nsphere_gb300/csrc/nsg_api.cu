@@ -272,9 +272,10 @@ static void free_buffers(nsg_ctx *c)
     }
     f(c->a0); f(c->inv); f(c->level); f(c->tile_counts); f(c->digit_tot); f(c->lc_idx); f(c->lc_early);
     f(c->red_part); f(c->stage_d);
-    f(c->split); f(c->bcnt); f(c->boff); f(c->bkey); f(c->bpay);
+    f(c->split); f(c->bcnt); f(c->boff); f(c->bkey); f(c->bpay); f(c->bidx);
     f(c->d_seg_start); f(c->d_bbase); f(c->seg_energy);
     c->nb_cap = 0;
+    c->bidx_cap = 0;
     c->cap = 0;
 }
 
@@ -439,6 +440,8 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
     if (e == cudaSuccess) e = cudaMemset(c->ctr, 0, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_ctr, sizeof(DevCounters));
     if (e == cudaSuccess && bucket_setup(c) != NSG_OK) e = cudaErrorInvalidValue;
+    if (e == cudaSuccess && fused_force_setup(c) != NSG_OK) e = cudaErrorInvalidValue;
+    if (e == cudaSuccess && fused_level0_setup(c) != NSG_OK) e = cudaErrorInvalidValue;
     if (e == cudaSuccess && lc_setup(c) != NSG_OK) e = cudaErrorInvalidValue;
     if (e == cudaSuccess && p->point_mass != 0.0)
         e = cudaMemcpy(&c->ctr->point_mass, &p->point_mass, sizeof(double), cudaMemcpyHostToDevice);
@@ -554,6 +557,14 @@ static int setup_segments(nsg_ctx *c, const int64_t *seg_n, int nseg)
         if (e == cudaSuccess) e = cudaMalloc((void **)&c->bpay, (size_t)nb * kBucketCap * 8);
         if (e != cudaSuccess) return cuda_err(c, e, "bucket buffers");
         c->nb_cap = nb;
+    }
+    const int64_t nbi = nb * (int64_t)fused_cap(c);
+    if (nbi > c->bidx_cap) {
+        F(c->bidx);
+        c->bidx_cap = 0;
+        e = cudaMalloc((void **)&c->bidx, (size_t)nbi * 4);
+        if (e != cudaSuccess) return cuda_err(c, e, "bucket index buffer");
+        c->bidx_cap = nbi;
     }
     F(c->d_seg_start); F(c->d_bbase); F(c->seg_energy);
     e = cudaMalloc((void **)&c->d_seg_start, start.size() * 8);

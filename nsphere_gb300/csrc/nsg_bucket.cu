@@ -58,11 +58,14 @@ __device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int l
     return b;
 }
 
+// IDX: the slot holds the particle's index only (bidx; the fused kernels re-read its
+// radius and id); otherwise (key, id << 32 | index) for k_bucket_sort.
+template <bool IDX>
 __global__ void __launch_bounds__(256)
 k_bucket_scatter(const double *__restrict__ r, const int32_t *__restrict__ id, int64_t n,
                  const uint64_t *__restrict__ S, Seg sg, int B, int cap,
                  unsigned int *__restrict__ cnt, uint64_t *__restrict__ bkey,
-                 uint64_t *__restrict__ bpay, DevCounters *ctr)
+                 uint64_t *__restrict__ bpay, uint32_t *__restrict__ bidx, DevCounters *ctr)
 {
     bool nan_seen = false;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
@@ -85,8 +88,12 @@ k_bucket_scatter(const double *__restrict__ r, const int32_t *__restrict__ id, i
         unsigned slot = base + __popc(peers & lanemask_lt());
         if (slot < (unsigned)cap) {
             int64_t at = (int64_t)b * cap + slot;
-            bkey[at] = key;
-            bpay[at] = ((uint64_t)(uint32_t)id[p] << 32) | (uint64_t)(uint32_t)p;
+            if (IDX) {
+                bidx[at] = (uint32_t)p;
+            } else {
+                bkey[at] = key;
+                bpay[at] = ((uint64_t)(uint32_t)id[p] << 32) | (uint64_t)(uint32_t)p;
+            }
         }
     }
     if (nan_seen) atomicOr(&ctr->status, NSG_ST_NAN);
@@ -420,8 +427,9 @@ int bucket_sort_perm(nsg_ctx *c)
     if (e != cudaSuccess) return cuda_err(c, e, "bucket count reset");
     {
         ProfScope ps(c, "bucket_scatter", (double)n * (8 + 4 + 16));
-        k_bucket_scatter<<<grid_for(c, n, 256, 8), 256, 0, s>>>(c->r[src], c->id[src], n, c->split, seg_table(c),
-                                                                 B, cap, c->bcnt, c->bkey, c->bpay, c->ctr);
+        k_bucket_scatter<false><<<grid_for(c, n, 256, 8), 256, 0, s>>>(c->r[src], c->id[src], n, c->split,
+                                                                        seg_table(c), B, cap, c->bcnt, c->bkey,
+                                                                        c->bpay, nullptr, c->ctr);
         k_bucket_scan<<<1, 1024, 0, s>>>(c->bcnt, nb, cap, c->boff, c->ctr);
     }
     {
@@ -432,6 +440,43 @@ int bucket_sort_perm(nsg_ctx *c)
     c->launches += 3;
     e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "bucket sort kernels");
+}
+
+// Entries a fused block sorts: twice the bucket target, 0 when the bucket target is
+// above what one block holds (the fused kernels are then not used).
+int fused_cap(const nsg_ctx *c)
+{
+    // blocks of 128, 256 or 512 threads holding 8 entries each
+    return (c->tune.bshift >= 9 && c->tune.bshift <= 11) ? (2 << c->tune.bshift) : 0;
+}
+
+bool use_fused(const nsg_ctx *c)
+{
+    return c->split_valid && c->p.sort_mode == 0 && fused_cap(c) > 0;
+}
+
+// Scatter and scan of the fused path: after this, bucket b's particle indices are in
+// c->bidx[b * cap ..] and its first sorted position in c->boff[b]; an overfull
+// bucket sets need_fallback (the fused kernels then return at once and the radix
+// sort with the two-kernel consumers runs instead).
+int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s)
+{
+    const int64_t n = c->n;
+    const int src = c->cur;
+    const int B = 1 << c->tune.bshift, cap = fused_cap(c);
+    const int nb = (int)c->nb_total;
+    cudaError_t e = cudaMemsetAsync(c->bcnt, 0, (size_t)nb * 4, s);
+    if (e != cudaSuccess) return cuda_err(c, e, "bucket count reset");
+    {
+        ProfScope ps(c, "bucket_scatter", (double)n * (8 + 4), s);
+        k_bucket_scatter<true><<<grid_for(c, n, 256, 8), 256, 0, s>>>(c->r[src], c->id[src], n, c->split,
+                                                                       seg_table(c), B, cap, c->bcnt, nullptr,
+                                                                       nullptr, c->bidx, c->ctr);
+        k_bucket_scan<<<1, 1024, 0, s>>>(c->bcnt, nb, cap, c->boff, c->ctr);
+    }
+    c->launches += 2;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "bucket scatter kernels");
 }
 
 int bucket_setup(nsg_ctx *c)

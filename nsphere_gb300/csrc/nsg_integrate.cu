@@ -29,7 +29,7 @@
 // evaluated once.
 #include <cstring>
 
-#include "nsg_internal.cuh"
+#include "nsg_fused.cuh"
 
 namespace nsg {
 
@@ -64,6 +64,8 @@ struct StepArgs {
     const uint32_t *lc_src;     // source index of each list entry when listed before the sort, or null
     const int8_t *pred;         // learned schedule: predicted level per position, or null
     Seg seg;                    // halos of an ensemble (ranks and sizes are per halo)
+    const unsigned *run_if;     // consumers of the radix fallback: return at once unless *run_if
+    uint32_t *perm_w;           // fused path: source index of each Levi-Civita particle's position
     // Substep sizes of each pass, identical for every particle, computed once on
     // the host with the same IEEE divisions as nsphere.c:1566-1577 (exact here:
     // h divided by powers of two): coarse N=1 halfKick h/2, midStep h;
@@ -146,15 +148,75 @@ __device__ __forceinline__ bool route_lc(const StepArgs &a, const Local &L, doub
     return (r > 1.0e-30) && (r < r_crit);
 }
 
+// Level-0 work of sorted position i (rank L within its halo) for the particle
+// (r, v, ell, idv) taken from source index s: write it into sorted order, write the
+// inverse map (nsphere.c:5789-5794) and the next sort's splitter, then -- unless it is
+// routed to Levi-Civita (nsphere.c:5804-5822), which another kernel handles --
+// compute its rank force numerator and start acceleration (nsphere.c:502-535) and
+// run adaptive level 0.  FUSED: the caller sorted in the block (no permutation
+// array), so a Levi-Civita particle leaves its source index in perm_w for the
+// chains, and joins their list here when it was not made before the sort.
+template <bool AUX, bool FUSED>
+__device__ __forceinline__ void level0_particle(const StepArgs &a, int64_t i, const Local &L, uint32_t s,
+                                                double r, double v, double ell, int32_t idv, double Mpt,
+                                                bool last)
+{
+    a.ell_out[i] = ell;
+    a.id_out[i] = idv;
+    if (AUX) a.aux_out[i] = a.aux_src[s];
+    a.inv[idv] = (int32_t)i;
+    write_splitter(a.split, a.seg, L, r);
+    if (route_lc(a, L, r, ell)) {
+        if (FUSED) {
+            a.perm_w[i] = s;
+            if (!a.ctr->lc_early_ok) {
+                const int slot = warp_append(true, &a.ctr->lc_count);
+                a.lc_idx[slot] = (uint32_t)i;
+            }
+        }
+        return;
+    }
+    const double gn = gnum_of(L.i, L.n, a.G, a.M, Mpt);
+    const double l2 = dmul(ell, ell);
+    const double af = acc_leap(r, gn, l2);
+    // learned schedule: a particle predicted to need level >= 1 goes straight to
+    // the level-parallel kernel, which tests every level from 0 upward
+    const bool fresh = (a.pred != nullptr) && !last && a.pred[i] >= 1;
+    double rc = 0.0, vc = 0.0, rf = 0.0, vf = 0.0;
+    bool done = false;
+    if (!fresh) {
+        micro_leap<false>(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
+        micro_leap<false>(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
+        const bool ok = converged<false>(rc, vc, rf, vf, rf, a);
+        const bool bad = !(finite_bits(rf) && finite_bits(vf));
+        done = ok || last || (bad && a.nf_stop);
+        if (done) {
+            double ro, vo;
+            select_out(a.out_type, rc, vc, rf, vf, ro, vo);
+            a.r_out[i] = ro;
+            a.v_out[i] = vo;
+            a.level[i] = ok ? 0 : kLevelNotConverged;
+            if (!ok) atomicOr(&a.ctr->status, bad ? (NSG_ST_NAN | NSG_ST_NOT_CONVERGED) : NSG_ST_NOT_CONVERGED);
+        }
+    }
+    const int q = warp_append(!done, &a.ctr->qcount[1]);
+    if (!done) {
+        a.r_out[i] = r;          // start values for the higher levels
+        a.v_out[i] = v;
+        a.a0[i] = af;
+        a.q_idx[q] = fresh ? ((uint32_t)i | kFreshBit) : (uint32_t)i;
+        a.q_r[q] = rf;
+        a.q_v[q] = vf;
+    }
+}
+
 // Fused pass after the sort, per sorted position i: gather the particle into
-// sorted order, write the inverse map (nsphere.c:5789-5794) and the next sort's
-// splitter, then -- unless it is routed to Levi-Civita (nsphere.c:5804-5822),
-// which the side stream handles -- compute its rank force numerator and start
-// acceleration (nsphere.c:502-535) and run adaptive level 0.  The pass is
+// sorted order through the permutation and do its level-0 work.  The pass is
 // FP64-bound, so the gather traffic hides under the arithmetic.
 template <bool AUX>
 __global__ void __launch_bounds__(512) k_gather_level0(StepArgs a)
 {
+    if (a.run_if && *a.run_if == 0u) return;   // fallback consumer: the fused kernel did the work
     const double Mpt = a.ctr->point_mass;
     const bool last = (a.nlev <= 1);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
@@ -162,45 +224,36 @@ __global__ void __launch_bounds__(512) k_gather_level0(StepArgs a)
         const uint32_t s = a.perm[i];
         const double r = a.r_src[s], v = a.v_src[s], ell = a.l_src[s];
         const int32_t idv = a.id_src[s];
-        a.ell_out[i] = ell;
-        a.id_out[i] = idv;
-        if (AUX) a.aux_out[i] = a.aux_src[s];
-        a.inv[idv] = (int32_t)i;
-        const Local L = local_of(a.seg, i, a.n);
-        write_splitter(a.split, a.seg, L, r);
-        if (route_lc(a, L, r, ell)) continue;
-        const double gn = gnum_of(L.i, L.n, a.G, a.M, Mpt);
-        const double l2 = dmul(ell, ell);
-        const double af = acc_leap(r, gn, l2);
-        // learned schedule: a particle predicted to need level >= 1 goes straight to
-        // the level-parallel kernel, which tests every level from 0 upward
-        const bool fresh = (a.pred != nullptr) && !last && a.pred[i] >= 1;
-        double rc = 0.0, vc = 0.0, rf = 0.0, vf = 0.0;
-        bool done = false;
-        if (!fresh) {
-            micro_leap<false>(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
-            micro_leap<false>(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
-            const bool ok = converged<false>(rc, vc, rf, vf, rf, a);
-            const bool bad = !(finite_bits(rf) && finite_bits(vf));
-            done = ok || last || (bad && a.nf_stop);
-            if (done) {
-                double ro, vo;
-                select_out(a.out_type, rc, vc, rf, vf, ro, vo);
-                a.r_out[i] = ro;
-                a.v_out[i] = vo;
-                a.level[i] = ok ? 0 : kLevelNotConverged;
-                if (!ok) atomicOr(&a.ctr->status, bad ? (NSG_ST_NAN | NSG_ST_NOT_CONVERGED) : NSG_ST_NOT_CONVERGED);
-            }
-        }
-        const int q = warp_append(!done, &a.ctr->qcount[1]);
-        if (!done) {
-            a.r_out[i] = r;          // start values for the higher levels
-            a.v_out[i] = v;
-            a.a0[i] = af;
-            a.q_idx[q] = fresh ? ((uint32_t)i | kFreshBit) : (uint32_t)i;
-            a.q_r[q] = rf;
-            a.q_v[q] = vf;
-        }
+        level0_particle<AUX, false>(a, i, local_of(a.seg, i, a.n), s, r, v, ell, idv, Mpt, last);
+    }
+}
+
+// The same with the near-sorted sort done in the block (nsg_fused.cuh): block b sorts
+// bucket b and does the level-0 work of its sorted positions off[b] ..; the sort's
+// integer and shared-memory work overlaps other blocks' FP64 work on the same SM.
+template <bool AUX, int T>
+__global__ void __launch_bounds__(T, T == 128 ? 6 : (T == 256 ? 3 : 1)) k_fused_level0(StepArgs a, FusedSort fs)
+{
+    if (a.ctr->need_fallback) return;
+    const int b = blockIdx.x;
+    const uint32_t m = fs.cnt[b];
+    if (m == 0u) return;
+    extern __shared__ __align__(16) unsigned char fsm[];
+    uint64_t *sr, *sv;
+    fused_bucket_sort<T>(fs, b, m, a.r_src, a.id_src, fsm, sr, sv);
+    const double Mpt = a.ctr->point_mass;
+    const bool last = (a.nlev <= 1);
+    const int h = halo_of_bucket(a.seg, b);
+    const int64_t hs = a.seg.nseg <= 1 ? 0 : a.seg.start[h];
+    const int64_t hn = a.seg.nseg <= 1 ? a.n : a.seg.start[h + 1] - hs;
+    const int64_t base = fs.off[b];
+    for (uint32_t j = threadIdx.x; j < m; j += T) {
+        const int64_t i = base + j;
+        const uint64_t e = sv[j];
+        const uint32_t s = (uint32_t)e;
+        const double r = entry_radius(sr[j], e, a.r_src);
+        const double v = a.v_src[s], ell = a.l_src[s];
+        level0_particle<AUX, true>(a, i, Local{i - hs, hn, h}, s, r, v, ell, entry_id(e), Mpt, last);
     }
 }
 
@@ -307,6 +360,7 @@ __global__ void __launch_bounds__(256) k_levels_lanes(StepArgs a, int G)
 // k_gather_level0); runs on the side stream right after the sort.
 __global__ void __launch_bounds__(256) k_lc_select(StepArgs a)
 {
+    if (a.run_if && *a.run_if == 0u) return;   // fallback consumer: the fused kernel listed them
     if (a.ctr->lc_early_ok) return;   // listed before the sort (k_lc_early_rank)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -1018,7 +1072,7 @@ k_kick_drift(double *__restrict__ r, double *__restrict__ v, const double *__res
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        double vi = dadd(v[i], dmul(dmul(0.5, a0[i]), dt));
+        double vi = dadd(v[i], dmul(half_exact(a0[i]), dt));
         v[i] = vi;
         r[i] = dadd(r[i], dmul(vi, dt));
     }
@@ -1064,6 +1118,8 @@ static StepArgs make_args(nsg_ctx *c)
     a.lc_src = nullptr;
     a.pred = nullptr;
     a.seg = seg_table(c);
+    a.run_if = nullptr;
+    a.perm_w = nullptr;
     return a;
 }
 
@@ -1092,16 +1148,98 @@ static uint64_t radius_key_host(double r)
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
+// Consumers of the radix fallback of a fused step (radix_fallback's tail): the
+// Levi-Civita selection (when listed after the sort) and the level-0 gather, both
+// through the radix permutation and gated by the fallback flag.
+struct Level0Tail {
+    StepArgs a;
+    bool select;
+};
+
+static void launch_gather_level0(nsg_ctx *c, const StepArgs &a, cudaStream_t st, const char *name)
+{
+    // algorithmic bytes: perm 4, gather r v ell id 28, write r v ell id 28, inv 4, level 1
+    ProfScope ps(c, name, (double)c->n * (4 + 28 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)), st);
+    const int th = c->tune.gl0_threads, grid = grid_for(c, c->n, th, c->tune.gl0_bps);
+    if (c->p.carry_aux) k_gather_level0<true><<<grid, th, 0, st>>>(a);
+    else k_gather_level0<false><<<grid, th, 0, st>>>(a);
+    c->launches += 1;
+}
+
+static int level0_tail(nsg_ctx *c, cudaStream_t st, const unsigned *run_if, void *arg)
+{
+    const Level0Tail *t = static_cast<const Level0Tail *>(arg);
+    StepArgs a = t->a;
+    a.perm = c->perm;
+    a.run_if = run_if;
+    if (t->select) {
+        ProfScope ps(c, "lc_select_fallback", (double)c->n * 20, st);
+        k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, st>>>(a);
+        c->launches += 1;
+    }
+    launch_gather_level0(c, a, st, "gather_level0_fallback");
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "level-0 fallback kernels");
+}
+
+// The fused sort + level 0 on stream st: index scatter and scan, one block per
+// bucket, then the radix fallback with its two-kernel consumers.
+static int fused_level0(nsg_ctx *c, StepArgs &a, cudaStream_t st, bool select)
+{
+    if (int rc = bucket_fused_prepare(c, st)) return rc;
+    a.perm = a.perm_w = c->vals[0];   // the radix fallback's even pass count ends in vals[0] too
+    const int cap = fused_cap(c);
+    const FusedSort fs{c->bidx, c->bcnt, c->boff, cap};
+    {
+        // algorithmic bytes: index 4, r id 12, v ell 16, write r v ell id 28, inv 4, level 1
+        ProfScope ps(c, "fused_level0", (double)c->n * (4 + 12 + 16 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)), st);
+        const int nb = (int)c->nb_total;
+        const size_t sm = fused_smem_bytes(cap);
+        if (cap == 4096) {
+            if (c->p.carry_aux) k_fused_level0<true, 512><<<nb, 512, sm, st>>>(a, fs);
+            else k_fused_level0<false, 512><<<nb, 512, sm, st>>>(a, fs);
+        } else if (cap == 2048) {
+            if (c->p.carry_aux) k_fused_level0<true, 256><<<nb, 256, sm, st>>>(a, fs);
+            else k_fused_level0<false, 256><<<nb, 256, sm, st>>>(a, fs);
+        } else {
+            if (c->p.carry_aux) k_fused_level0<true, 128><<<nb, 128, sm, st>>>(a, fs);
+            else k_fused_level0<false, 128><<<nb, 128, sm, st>>>(a, fs);
+        }
+        c->launches += 1;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(c, e, "fused level-0 kernel");
+    Level0Tail t{a, select};
+    return radix_fallback(c, st, level0_tail, &t);
+}
+
+int fused_level0_setup(nsg_ctx *c)
+{
+    cudaError_t e = cudaSuccess;
+#define NSG_ATTR(AUXV, TV)                                                                   \
+    if (e == cudaSuccess)                                                                    \
+        e = cudaFuncSetAttribute(k_fused_level0<AUXV, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                 (int)fused_smem_bytes(TV * kFusedItems));
+    NSG_ATTR(false, 128) NSG_ATTR(true, 128) NSG_ATTR(false, 256) NSG_ATTR(true, 256) NSG_ATTR(false, 512)
+    NSG_ATTR(true, 512)
+#undef NSG_ATTR
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "fused level-0 attributes");
+}
+
 int integrate_adaptive(nsg_ctx *c)
 {
     const bool lc = ((c->p.method == NSG_METHOD_ADAPTIVE_LC || c->p.method == NSG_METHOD_FULL_LC) &&
                      c->p.lc_rule != NSG_LC_OFF);
     // fixed-radius rule: the Levi-Civita list is made before the sort
     const bool early = lc && c->p.lc_rule == NSG_LC_RADIUS;
-    if (!early)
+    const bool learned = (c->p.sched == NSG_SCHED_LEARNED);
+    // the sort runs inside the level-0 kernel unless something needs the permutation
+    // before it: the scheduler's features, or a Levi-Civita list made after the sort
+    const bool fz = use_fused(c) && !learned && !c->mlp_collect && (early || !lc);
+    if (!early && !fz)
         if (int rc = sort_perm(c)) return rc;
     StepArgs a = make_args(c);
-    const bool learned = (c->p.sched == NSG_SCHED_LEARNED) && a.nlev > 1;
+    const bool learned_lv = learned && a.nlev > 1;
     cudaStream_t s = c->stream;
     cudaError_t e;
     // reset queue counters (lc_count, qcount[], lc_next, lc_cand, lc_early_ok lead DevCounters)
@@ -1136,14 +1274,18 @@ int integrate_adaptive(nsg_ctx *c)
             ae.lc_src = lsrc;
             launch_levi_civita(c, ae, s);
         }
-        const cudaStream_t keep = c->stream;
-        c->stream = c->side;
-        const int rc = sort_perm(c);
-        c->stream = keep;
-        if (rc) return rc;
-        a.perm = c->perm;
         ls = c->side;
-        {
+        if (fz) {
+            // sort + level 0 in one kernel; it lists the Levi-Civita particles itself
+            // when the list before the sort overflowed
+            if (int rc = fused_level0(c, a, ls, true)) return rc;
+        } else {
+            const cudaStream_t keep = c->stream;
+            c->stream = c->side;
+            const int rc = sort_perm(c);
+            c->stream = keep;
+            if (rc) return rc;
+            a.perm = c->perm;
             ProfScope ps(c, "lc_select", (double)c->n * 20, ls);
             k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, ls>>>(a);   // returns at once unless the list overflowed
             c->launches += 1;
@@ -1167,25 +1309,20 @@ int integrate_adaptive(nsg_ctx *c)
         ls = c->side;
         ProfScope ps(c, "levi_civita", 0.0);
         launch_levi_civita(c, a, s);
+    } else if (fz) {
+        if (int rc = fused_level0(c, a, s, false)) return rc;
     }
     // the scheduler's features and predictions run beside the Levi-Civita chains too
-    if (learned)
+    if (learned_lv)
         if (int rc = mlp_predict_sorted(c, &a.pred, ls)) return rc;
     if (c->mlp_collect)
         if (int rc = mlp_features_sorted(c, ls)) return rc;
-    {
-        // algorithmic bytes: perm 4, gather r v ell id 28, write r v ell id 28, inv 4, level 1
-        ProfScope ps(c, "gather_level0", (double)c->n * (4 + 28 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)), ls);
-        const int th = c->tune.gl0_threads, grid = grid_for(c, c->n, th, c->tune.gl0_bps);
-        if (c->p.carry_aux) k_gather_level0<true><<<grid, th, 0, ls>>>(a);
-        else k_gather_level0<false><<<grid, th, 0, ls>>>(a);
-        c->launches += 1;
-    }
+    if (!fz) launch_gather_level0(c, a, ls, "gather_level0");
     if (a.nlev > 1) {
         ProfScope ps(c, "leap_levels", 0.0, ls);
         int G = 1;
-        while (G < (learned ? a.nlev + 1 : a.nlev - 1)) G <<= 1;
-        if (learned) k_levels_lanes<true><<<c->num_sms * c->tune.lanes_bps, 256, 0, ls>>>(a, G);
+        while (G < (learned_lv ? a.nlev + 1 : a.nlev - 1)) G <<= 1;
+        if (learned_lv) k_levels_lanes<true><<<c->num_sms * c->tune.lanes_bps, 256, 0, ls>>>(a, G);
         else k_levels_lanes<false><<<c->num_sms * c->tune.lanes_bps, 256, 0, ls>>>(a, G);
         c->launches += 1;
     }

@@ -24,12 +24,13 @@ constexpr int kRadixItems = 16;       // keys per thread per tile
 constexpr int kRadixTile = kRadixThreads * kRadixItems;
 constexpr int kReduceBlocks = 1024;   // fixed block count of energy partial sums
 constexpr int kBucketCap = 6144;      // entries one bucket block sorts (1024 threads x 6)
+constexpr int kFusedCapMax = 4096;    // entries one fused sort block holds (512 threads x 8)
 
 // Launch shapes chosen by the autotuner (nsg_tune.cu); defaults measured on GB300.
 struct Tune {
     int gl0_threads = 256;   // k_gather_level0 block size
     int gl0_bps = 8;         // k_gather_level0 blocks per SM
-    int bshift = 11;         // near-sorted sort: 2^bshift sorted positions per splitter
+    int bshift = 10;         // near-sorted sort: 2^bshift sorted positions per splitter
     int lanes_bps = 4;       // k_levels_lanes blocks per SM
 };
 
@@ -113,6 +114,8 @@ struct nsg_ctx {
     bool split_valid = false;
     unsigned int *bcnt = nullptr, *boff = nullptr;  // [nb]
     uint64_t *bkey = nullptr, *bpay = nullptr;      // [nb * kBucketCap]
+    uint32_t *bidx = nullptr;                       // [nb * fused_cap] (fused path)
+    int64_t bidx_cap = 0;                           // entries allocated in bidx
 
     // leapfrog level queues (ping-pong) and the Levi-Civita list
     uint32_t *q_idx[2] = {nullptr, nullptr};
@@ -183,12 +186,19 @@ __device__ __forceinline__ bool open_between(double r, double lo, double hi)
     const long long b = dbits(r);
     return b > dbits(lo) && b < dbits(hi);
 }
+// Rare operand paths behind calls.  A branch whose other side issues FP64
+// instructions is if-converted by the compiler -- both sides are computed and one is
+// selected -- so an inline slow path costs its FP64 issue slots on every call; a call
+// cannot be predicated that way, so its instructions run only when it is taken.
+static __device__ __noinline__ double dmul_call(double a, double b) { return __dmul_rn(a, b); }
+static __device__ __noinline__ double dadd_call(double a, double b) { return __dadd_rn(a, b); }
+
 // x + 1e-30 for x >= +0 or NaN.  From x = 2^-46 up, 1e-30 is below half an ulp of x
 // (2^-99), so the sum rounds to x; only smaller x take the FP64 addition.
 __device__ __forceinline__ double add_1em30(double x)
 {
     if (dbits(x) >= (977ll << 52)) return x;
-    return dadd(x, 1.0e-30);
+    return dadd_call(x, 1.0e-30);
 }
 // 4 x: for a normal x whose product stays normal the exponent field rises by two
 // (exact, as the multiplication); other x take the FP64 multiplication.
@@ -196,7 +206,7 @@ __device__ __forceinline__ double mul4(double x)
 {
     const long long b = dbits(x);
     if (((unsigned)(b >> 52) & 0x7ffu) - 1u < 2044u) return __longlong_as_double(b + (2ll << 52));
-    return dmul(4.0, x);
+    return dmul_call(4.0, x);
 }
 // RN(x / y) < tol, decided without the division.  RN is monotonic, and the quotient
 // of two doubles is never halfway between two doubles (that would take a 54-bit odd
@@ -260,13 +270,34 @@ template <bool HW>
 __device__ __forceinline__ double ddivx(double a, double b) { return HW ? div_rn_hw(a, b) : div_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return div_rn(a, b); }
 
-// -(G) * (i / n) * M (+ the point-mass term when present), nsphere.c:513.
+// -(G) * (i / n) * M (+ the point-mass term when present), nsphere.c:513.  With
+// G = M = 1 (the units of the benchmark halos) both products are exact: the result
+// is the quotient with its sign flipped, and no FP64 instruction is issued (the
+// tests of G, M and Mpt compare bit patterns on the integer pipe).
+static __device__ __noinline__ double gnum_general(double q, double G, double M, double Mpt)
+{
+    double g = __dmul_rn(__dmul_rn(-G, q), M);
+    if (Mpt != 0.0) g = __dsub_rn(g, __dmul_rn(G, Mpt));
+    return g;
+}
+
 template <bool HW = false>
 __device__ __forceinline__ double gnum_of(int64_t i, int64_t n, double G, double M, double Mpt)
 {
-    double g = dmul(dmul(-G, ddivx<HW>(u32_to_double((uint32_t)i), u32_to_double((uint32_t)n))), M);
-    if (Mpt != 0.0) g = dsub(g, dmul(G, Mpt));
-    return g;
+    const double q = ddivx<HW>(u32_to_double((uint32_t)i), u32_to_double((uint32_t)n));
+    constexpr long long kOne = 0x3ff0000000000000ll;
+    if (dbits(G) == kOne && dbits(M) == kOne && (dbits(Mpt) << 1) == 0)   // Mpt == 0.0
+        return __longlong_as_double(dbits(q) ^ (long long)0x8000000000000000ull);
+    return gnum_general(q, G, M, Mpt);
+}
+
+// 0.5 x: for a normal x whose half stays normal the exponent field falls by one
+// (exact, as the multiplication); other x take the FP64 multiplication.
+__device__ __forceinline__ double half_exact(double x)
+{
+    const long long b = dbits(x);
+    if (((unsigned)(b >> 52) & 0x7ffu) - 2u < 2045u) return __longlong_as_double(b - (1ll << 52));
+    return dmul_call(0.5, x);
 }
 
 // gravity + centrifugal: gnum/(r*r) + l2/(r*r*r), nsphere.c:502-535.
@@ -376,6 +407,14 @@ int integrate_adaptive(nsg_ctx *c);                   // method 3 / 5: sort_perm
 int kdk_first_half(nsg_ctx *c);                       // kick (a0 of the current rank) + drift
 int compute_energy(nsg_ctx *c);                       // K, W of the sorted live copy
 int bucket_sort_perm(nsg_ctx *c);                     // near-sorted fast path (sets need_fallback)
+int fused_cap(const nsg_ctx *c);                      // entries of a fused sort block (0: fused path off)
+int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s); // scatter indices + scan for the fused kernels
+bool use_fused(const nsg_ctx *c);                     // the sort of this step runs inside its consumer
+// Launches the radix sort and then `tail` on stream s so that they run only when
+// need_fallback is set: in a captured step as the body of a conditional graph node,
+// otherwise eagerly with kernels that return at once (tail receives the flag to test).
+int radix_fallback(nsg_ctx *c, cudaStream_t s, int (*tail)(nsg_ctx *, cudaStream_t, const unsigned *, void *),
+                   void *arg);
 inline Seg seg_table(const nsg_ctx *c) { return Seg{c->d_seg_start, c->d_bbase, c->nseg, c->tune.bshift}; }
 void drop_graph(nsg_ctx *c);                          // forget the captured step graph
 int set_halos(nsg_ctx *c, const int64_t *seg_n, int nseg);  // halo table + bucket layout
@@ -393,6 +432,8 @@ int mlp_features_sorted(nsg_ctx *c, cudaStream_t st);  // features of the sort (
 int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)
 void mlp_free(nsg_ctx *c);
 int bucket_setup(nsg_ctx *c);
+int fused_force_setup(nsg_ctx *c);   // shared-memory attributes of the fused sort kernels
+int fused_level0_setup(nsg_ctx *c);
 int lc_setup(nsg_ctx *c);            // Levi-Civita kernel attributes
 int lc_probe_substep(double *cycles_split, double *cycles_zero_gravity, double *cycles_dual);
 int launch_gather(nsg_ctx *c, const int32_t *d_ids, int k, double *d_out, int32_t *d_rank);

@@ -14,7 +14,7 @@
 // (r, id) total order.  Each pass: per-tile digit counts -> per-digit scan ->
 // stable warp-level ranking (match.any) and scatter.  No kernel waits on another
 // block, so no spin loops.
-#include "nsg_internal.cuh"
+#include "nsg_fused.cuh"
 
 namespace nsg {
 
@@ -223,8 +223,10 @@ k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
                     double *__restrict__ r1, double *__restrict__ v1, double *__restrict__ l1,
                     int32_t *__restrict__ id1, double *__restrict__ x1,
                     double *__restrict__ a0, int32_t *__restrict__ inv, uint64_t *__restrict__ split,
-                    double G, double M, double dt, const DevCounters *__restrict__ ctr, Seg sg)
+                    double G, double M, double dt, const DevCounters *__restrict__ ctr, Seg sg,
+                    const unsigned *__restrict__ run_if)
 {
+    if (run_if && *run_if == 0u) return;   // fallback consumer: the fused kernel did the work
     const double Mpt = ctr->point_mass;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
          p += (int64_t)gridDim.x * blockDim.x) {
@@ -234,7 +236,55 @@ k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
         int32_t idv = id0[s];
         double gn = gnum_of(L.i, L.n, G, M, Mpt);
         double acc = acc_leap(r, gn, dmul(l, l));
-        if (KICK) v = dadd(v, dmul(dmul(0.5, acc), dt));
+        if (KICK) v = dadd(v, dmul(half_exact(acc), dt));
+        r1[p] = r;
+        v1[p] = v;
+        l1[p] = l;
+        id1[p] = idv;
+        if (AUX) x1[p] = x0[s];
+        inv[idv] = (int32_t)p;
+        a0[p] = acc;
+        write_splitter(split, sg, L, r);
+    }
+}
+
+// The same pass with the near-sorted sort done in the block (nsg_fused.cuh): block b
+// sorts bucket b and writes its sorted positions off[b] .. off[b] + cnt[b] - 1.
+template <bool AUX, bool KICK, int T>
+__global__ void __launch_bounds__(T, T == 128 ? 8 : (T == 256 ? 4 : 2))
+k_fused_rank_force(FusedSort fs, int64_t n,
+                   const double *__restrict__ r0, const double *__restrict__ v0,
+                   const double *__restrict__ l0, const int32_t *__restrict__ id0,
+                   const double *__restrict__ x0,
+                   double *__restrict__ r1, double *__restrict__ v1, double *__restrict__ l1,
+                   int32_t *__restrict__ id1, double *__restrict__ x1,
+                   double *__restrict__ a0, int32_t *__restrict__ inv, uint64_t *__restrict__ split,
+                   double G, double M, double dt, const DevCounters *__restrict__ ctr, Seg sg)
+{
+    if (ctr->need_fallback) return;
+    const int b = blockIdx.x;
+    const uint32_t m = fs.cnt[b];
+    if (m == 0u) return;
+    extern __shared__ __align__(16) unsigned char fsm[];
+    uint64_t *sr, *sv;
+    fused_bucket_sort<T>(fs, b, m, r0, id0, fsm, sr, sv);
+    const double Mpt = ctr->point_mass;
+    const int h = halo_of_bucket(sg, b);
+    const int64_t hs = sg.nseg <= 1 ? 0 : sg.start[h];
+    const int64_t hn = sg.nseg <= 1 ? n : sg.start[h + 1] - hs;
+    const int64_t base = fs.off[b];
+    for (uint32_t j = threadIdx.x; j < m; j += T) {
+        const int64_t p = base + j;
+        const Local L{p - hs, hn, h};
+        const uint64_t e = sv[j];
+        const uint32_t s = (uint32_t)e;
+        const int32_t idv = entry_id(e);
+        const double r = entry_radius(sr[j], e, r0);
+        double v = v0[s];
+        const double l = l0[s];
+        const double gn = gnum_of(L.i, L.n, G, M, Mpt);
+        const double acc = acc_leap(r, gn, dmul(l, l));
+        if (KICK) v = dadd(v, dmul(half_exact(acc), dt));
         r1[p] = r;
         v1[p] = v;
         l1[p] = l;
@@ -367,9 +417,60 @@ __global__ void k_radix_cond(cudaGraphConditionalHandle h, const DevCounters *__
     if (threadIdx.x == 0) cudaGraphSetConditional(h, ctr->need_fallback ? 1u : 0u);
 }
 
+int radix_fallback(nsg_ctx *c, cudaStream_t s, int (*tail)(nsg_ctx *, cudaStream_t, const unsigned *, void *),
+                   void *arg)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr);
+    if (e != cudaSuccess) return cuda_err(c, e, "capture status");
+    int kb = 0;
+    const int npass = 8 + (c->nseg > 1 ? 2 : 0);
+    if (cs != cudaStreamCaptureStatusActive || !c->cond_nodes) {
+        if (int rc = launch_radix(c, s, &kb)) return rc;
+        c->launches += 1 + npass * 4;
+        c->perm = c->vals[kb];
+        if (tail)
+            if (int rc = tail(c, s, &c->ctr->need_fallback, arg)) return rc;
+        return NSG_OK;
+    }
+    // In a captured step the radix kernels (and the consumer that goes with them) sit
+    // in the body of a conditional node that a one-thread kernel opens only when the
+    // near-sorted path overflowed: the 33-41 launches that would return at once cost
+    // nothing.
+    cudaGraphConditionalHandle h;
+    e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+    if (e != cudaSuccess) return cuda_err(c, e, "conditional handle");
+    k_radix_cond<<<1, 32, 0, s>>>(h, c->ctr);
+    c->launches += 1;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return cuda_err(c, e, "capture dependencies");
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp);
+    if (e != cudaSuccess) return cuda_err(c, e, "conditional node");
+    e = cudaStreamBeginCaptureToGraph(c->body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return cuda_err(c, e, "conditional body capture");
+    int rc = launch_radix(c, c->body, &kb);
+    c->perm = c->vals[kb];
+    if (!rc && tail) rc = tail(c, c->body, nullptr, arg);
+    cudaGraph_t bg = nullptr;
+    e = cudaStreamEndCapture(c->body, &bg);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_err(c, e, "conditional body capture");
+    e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return cuda_err(c, e, "capture dependencies");
+    return NSG_OK;
+}
+
 int sort_perm(nsg_ctx *c)
 {
-    const int64_t n = c->n;
     cudaStream_t s = c->stream;
     // near-sorted fast path when the array is in the order of a previous sort;
     // the radix kernels below run only if it overflowed (or it was not used)
@@ -380,71 +481,80 @@ int sort_perm(nsg_ctx *c)
         cudaError_t e = cudaMemsetAsync(&c->ctr->need_fallback, 1, sizeof(unsigned), s);
         if (e != cudaSuccess) return cuda_err(c, e, "fallback flag");
     }
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr);
-    if (e != cudaSuccess) return cuda_err(c, e, "capture status");
-    int kb = 0;
-    if (cs != cudaStreamCaptureStatusActive || !c->cond_nodes) {
-        if (int rc = launch_radix(c, s, &kb)) return rc;
-        const int npass = 8 + (c->nseg > 1 ? 2 : 0);
-        c->launches += 1 + npass * 4;
-    } else {
-        // In a captured step the radix kernels sit in the body of a conditional node
-        // that a one-thread kernel opens only when the near-sorted path overflowed:
-        // the 33-41 launches that would return at once cost nothing.
-        cudaGraphConditionalHandle h;
-        e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
-        if (e != cudaSuccess) return cuda_err(c, e, "conditional handle");
-        k_radix_cond<<<1, 32, 0, s>>>(h, c->ctr);
-        c->launches += 1;
-        const cudaGraphNode_t *deps = nullptr;
-        size_t nd = 0;
-        e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd);
-        if (e != cudaSuccess) return cuda_err(c, e, "capture dependencies");
-        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-        cp.conditional.handle = h;
-        cp.conditional.type = cudaGraphCondTypeIf;
-        cp.conditional.size = 1;
-        cudaGraphNode_t node;
-        e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp);
-        if (e != cudaSuccess) return cuda_err(c, e, "conditional node");
-        e = cudaStreamBeginCaptureToGraph(c->body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                          cudaStreamCaptureModeRelaxed);
-        if (e != cudaSuccess) return cuda_err(c, e, "conditional body capture");
-        const int rc = launch_radix(c, c->body, &kb);
-        cudaGraph_t bg = nullptr;
-        e = cudaStreamEndCapture(c->body, &bg);
-        if (rc) return rc;
-        if (e != cudaSuccess) return cuda_err(c, e, "conditional body capture");
-        e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-        if (e != cudaSuccess) return cuda_err(c, e, "capture dependencies");
-    }
-    c->perm = c->vals[kb];
-    return NSG_OK;
+    return radix_fallback(c, s, nullptr, nullptr);
 }
 
-static int gather(nsg_ctx *c, bool kick)
+// The two-kernel consumer: k_gather_rank_force through c->perm on stream s (run_if:
+// return at once unless *run_if is set).
+static int launch_gather(nsg_ctx *c, bool kick, cudaStream_t s, const unsigned *run_if)
 {
     const int64_t n = c->n;
     const int src = c->cur, dst = 1 - c->cur;
-    cudaStream_t s = c->stream;
     const Seg sg = seg_table(c);
-    ProfScope ps(c, kick ? "gather_kick" : "rank_force",
-                 (double)n * (4 + 28 + 28 + 8 + 4 + (c->p.carry_aux ? 16 : 0)));
+    ProfScope ps(c, run_if ? (kick ? "gather_kick_fallback" : "rank_force_fallback") : (kick ? "gather_kick" : "rank_force"),
+                 (double)n * (4 + 28 + 28 + 8 + 4 + (c->p.carry_aux ? 16 : 0)), s);
     const int grid = grid_for(c, n, 256, 8);
 #define NSG_GATHER(AUXV, KICKV)                                                                   \
     k_gather_rank_force<AUXV, KICKV><<<grid, 256, 0, s>>>(                                        \
         c->perm, n, c->r[src], c->vr[src], c->ell[src], c->id[src], c->aux[src], c->r[dst],      \
         c->vr[dst], c->ell[dst], c->id[dst], c->aux[dst], c->a0, c->inv, c->split, c->p.G,       \
-        c->p.M_total, c->p.dt, c->ctr, sg)
+        c->p.M_total, c->p.dt, c->ctr, sg, run_if)
     if (c->p.carry_aux) { if (kick) NSG_GATHER(true, true); else NSG_GATHER(true, false); }
     else { if (kick) NSG_GATHER(false, true); else NSG_GATHER(false, false); }
 #undef NSG_GATHER
     c->launches += 1;
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_err(c, e, "gather kernel");
-    c->cur = dst;
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "gather kernel");
+}
+
+static int gather_tail(nsg_ctx *c, cudaStream_t s, const unsigned *run_if, void *arg)
+{
+    return launch_gather(c, *static_cast<const bool *>(arg), s, run_if);
+}
+
+template <int T>
+static void launch_fused_force(nsg_ctx *c, bool kick, cudaStream_t s)
+{
+    const int64_t n = c->n;
+    const int src = c->cur, dst = 1 - c->cur;
+    const int cap = fused_cap(c);
+    const FusedSort fs{c->bidx, c->bcnt, c->boff, cap};
+    const size_t sm = fused_smem_bytes(cap);
+    const int nb = (int)c->nb_total;
+#define NSG_FUSED(AUXV, KICKV)                                                                          \
+    k_fused_rank_force<AUXV, KICKV, T><<<nb, T, sm, s>>>(                                               \
+        fs, n, c->r[src], c->vr[src], c->ell[src], c->id[src], c->aux[src], c->r[dst], c->vr[dst],      \
+        c->ell[dst], c->id[dst], c->aux[dst], c->a0, c->inv, c->split, c->p.G, c->p.M_total, c->p.dt,  \
+        c->ctr, seg_table(c))
+    if (c->p.carry_aux) { if (kick) NSG_FUSED(true, true); else NSG_FUSED(true, false); }
+    else { if (kick) NSG_FUSED(false, true); else NSG_FUSED(false, false); }
+#undef NSG_FUSED
+}
+
+static int sort_gather(nsg_ctx *c, bool kick)
+{
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    if (use_fused(c)) {
+        if (int rc = bucket_fused_prepare(c, s)) return rc;
+        {
+            // algorithmic bytes: index 4, r id 12, v ell 16, write r v ell id 28, a0 8, inv 4
+            ProfScope ps(c, kick ? "fused_kick" : "fused_force", (double)n * (4 + 12 + 16 + 28 + 8 + 4 +
+                                                                               (c->p.carry_aux ? 16 : 0)), s);
+            if (fused_cap(c) == 4096) launch_fused_force<512>(c, kick, s);
+            else if (fused_cap(c) == 2048) launch_fused_force<256>(c, kick, s);
+            else launch_fused_force<128>(c, kick, s);
+            c->launches += 1;
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_err(c, e, "fused sort kernel");
+        bool k = kick;
+        if (int rc = radix_fallback(c, s, gather_tail, &k)) return rc;
+    } else {
+        if (int rc = sort_perm(c)) return rc;
+        if (int rc = launch_gather(c, kick, s, nullptr)) return rc;
+    }
+    c->cur = 1 - c->cur;
     c->sorted = true;
     c->inv_valid = true;
     c->split_valid = true;
@@ -453,14 +563,26 @@ static int gather(nsg_ctx *c, bool kick)
 
 int sort_state(nsg_ctx *c)
 {
-    if (int rc = sort_perm(c)) return rc;
-    return gather(c, false);
+    return sort_gather(c, false);
 }
 
 int sort_state_kick(nsg_ctx *c)
 {
-    if (int rc = sort_perm(c)) return rc;
-    return gather(c, true);
+    return sort_gather(c, true);
+}
+
+int fused_force_setup(nsg_ctx *c)
+{
+    cudaError_t e = cudaSuccess;
+#define NSG_ATTR(AUXV, KICKV, TV)                                                                       \
+    if (e == cudaSuccess)                                                                               \
+        e = cudaFuncSetAttribute(k_fused_rank_force<AUXV, KICKV, TV>,                                    \
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem_bytes(2 * TV * 4));
+    NSG_ATTR(false, false, 128) NSG_ATTR(false, true, 128) NSG_ATTR(true, false, 128) NSG_ATTR(true, true, 128)
+    NSG_ATTR(false, false, 256) NSG_ATTR(false, true, 256) NSG_ATTR(true, false, 256) NSG_ATTR(true, true, 256)
+    NSG_ATTR(false, false, 512) NSG_ATTR(false, true, 512) NSG_ATTR(true, false, 512) NSG_ATTR(true, true, 512)
+#undef NSG_ATTR
+    return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "fused sort attributes");
 }
 
 int compute_energy(nsg_ctx *c)

@@ -377,9 +377,10 @@ int nsg_profile_read(nsg_ctx *ctx, nsg_kernel_stat *stats, int max, int *count);
 
 /* Launch-shape tuning (no counterpart in the reference, whose step runs on CPU
  * threads).  vals[4] = {gather_level0 threads (128|256|512), gather_level0 blocks
- * per SM (1..64), log2 of sorted positions per bucket (8..12), level-kernel blocks
- * per SM (1..64)}.  Shapes change no arithmetic: results are identical for every
- * setting. */
+ * per SM (1..64), log2 of sorted positions per bucket (8..12; 9..11 sort inside the
+ * kernel that consumes the sort, 8 and 12 with a separate bucket-sort kernel),
+ * level-kernel blocks per SM (1..64)}.  Shapes change no arithmetic: results are
+ * identical for every setting. */
 int nsg_tune_get(nsg_ctx *ctx, int32_t *vals, int count);
 int nsg_tune_set(nsg_ctx *ctx, const int32_t *vals, int count);
 /* Times candidate shapes over `steps` steps of the resident state, one knob at a

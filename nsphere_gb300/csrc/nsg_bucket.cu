@@ -58,14 +58,11 @@ __device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int l
     return b;
 }
 
-// IDX: the slot holds the particle's index only (bidx; the fused kernels re-read its
-// radius and id); otherwise (key, id << 32 | index) for k_bucket_sort.
-template <bool IDX>
 __global__ void __launch_bounds__(256)
 k_bucket_scatter(const double *__restrict__ r, const int32_t *__restrict__ id, int64_t n,
                  const uint64_t *__restrict__ S, Seg sg, int B, int cap,
                  unsigned int *__restrict__ cnt, uint64_t *__restrict__ bkey,
-                 uint64_t *__restrict__ bpay, uint32_t *__restrict__ bidx, DevCounters *ctr)
+                 uint64_t *__restrict__ bpay, DevCounters *ctr)
 {
     bool nan_seen = false;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
@@ -88,13 +85,71 @@ k_bucket_scatter(const double *__restrict__ r, const int32_t *__restrict__ id, i
         unsigned slot = base + __popc(peers & lanemask_lt());
         if (slot < (unsigned)cap) {
             int64_t at = (int64_t)b * cap + slot;
-            if (IDX) {
-                bidx[at] = (uint32_t)p;
-            } else {
-                bkey[at] = key;
-                bpay[at] = ((uint64_t)(uint32_t)id[p] << 32) | (uint64_t)(uint32_t)p;
-            }
+            bkey[at] = key;
+            bpay[at] = ((uint64_t)(uint32_t)id[p] << 32) | (uint64_t)(uint32_t)p;
         }
+    }
+    if (nan_seen) atomicOr(&ctr->status, NSG_ST_NAN);
+}
+
+// Index scatter of the fused path, 8 particles per thread: a block takes 2048
+// consecutive positions, loads all their radii first (coalesced), then for each
+// particle tests its home bucket with both bounding splitters read at once -- the
+// common case, a particle that did not cross a splitter -- and walks or searches
+// only when it did.  A warp whose particles all fall in one bucket appends them
+// with one atomic, in position order.
+constexpr int kScatterItems = 8;
+
+__global__ void __launch_bounds__(256)
+k_bucket_scatter_idx(const double *__restrict__ r, int64_t n, const uint64_t *__restrict__ S, Seg sg, int bshift,
+                     int cap, unsigned int *__restrict__ cnt, uint32_t *__restrict__ bidx, DevCounters *ctr)
+{
+    const int64_t p0 = (int64_t)blockIdx.x * (256 * kScatterItems);
+    double rv[kScatterItems];
+#pragma unroll
+    for (int j = 0; j < kScatterItems; j++) {
+        const int64_t p = p0 + j * 256 + threadIdx.x;
+        rv[j] = p < n ? r[p] : 0.0;
+    }
+    bool nan_seen = false;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int j = 0; j < kScatterItems; j++) {
+        const int64_t p = p0 + j * 256 + threadIdx.x;
+        if (p0 + j * 256 >= n) break;                  // the rest of the block is past the end (uniform)
+        const bool valid = p < n;
+        int b = -1;
+        if (valid) {
+            const double rp = rv[j];
+            nan_seen |= (rp != rp);
+            const uint64_t key = radius_key(rp);
+            const Local L = local_of(sg, p, n);
+            const int lo = sg.bbase[L.h], hi = sg.bbase[L.h + 1];
+            int home = lo + (int)(L.i >> bshift);
+            if (home >= hi) home = hi - 1;
+            const uint64_t s0 = S[home];
+            const uint64_t s1 = home + 1 < hi ? S[home + 1] : ~0ull;
+            if (s0 <= key && (key < s1 || home + 1 >= hi)) b = home;
+            else b = find_bucket(S, lo, hi, key, home);
+        }
+        const unsigned act = __ballot_sync(0xffffffffu, valid);
+        if (act == 0u) continue;                       // lane 0 holds the warp's first position
+        const int b0 = __shfl_sync(0xffffffffu, b, 0);
+        unsigned slot;
+        if (__all_sync(0xffffffffu, !valid || b == b0)) {
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(&cnt[b0], (unsigned)__popc(act));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            slot = base + __popc(act & lanemask_lt());
+        } else {
+            const unsigned peers = __match_any_sync(0xffffffffu, b);
+            const int leader = __ffs(peers) - 1;
+            unsigned base = 0;
+            if (lane == leader && valid) base = atomicAdd(&cnt[b], (unsigned)__popc(peers));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            slot = base + __popc(peers & lanemask_lt());
+        }
+        if (valid && slot < (unsigned)cap) bidx[(int64_t)b * cap + slot] = (uint32_t)p;
     }
     if (nan_seen) atomicOr(&ctr->status, NSG_ST_NAN);
 }
@@ -427,9 +482,8 @@ int bucket_sort_perm(nsg_ctx *c)
     if (e != cudaSuccess) return cuda_err(c, e, "bucket count reset");
     {
         ProfScope ps(c, "bucket_scatter", (double)n * (8 + 4 + 16));
-        k_bucket_scatter<false><<<grid_for(c, n, 256, 8), 256, 0, s>>>(c->r[src], c->id[src], n, c->split,
-                                                                        seg_table(c), B, cap, c->bcnt, c->bkey,
-                                                                        c->bpay, nullptr, c->ctr);
+        k_bucket_scatter<<<grid_for(c, n, 256, 8), 256, 0, s>>>(c->r[src], c->id[src], n, c->split, seg_table(c),
+                                                                 B, cap, c->bcnt, c->bkey, c->bpay, c->ctr);
         k_bucket_scan<<<1, 1024, 0, s>>>(c->bcnt, nb, cap, c->boff, c->ctr);
     }
     {
@@ -463,15 +517,15 @@ int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s)
 {
     const int64_t n = c->n;
     const int src = c->cur;
-    const int B = 1 << c->tune.bshift, cap = fused_cap(c);
+    const int cap = fused_cap(c);
     const int nb = (int)c->nb_total;
     cudaError_t e = cudaMemsetAsync(c->bcnt, 0, (size_t)nb * 4, s);
     if (e != cudaSuccess) return cuda_err(c, e, "bucket count reset");
     {
         ProfScope ps(c, "bucket_scatter", (double)n * (8 + 4), s);
-        k_bucket_scatter<true><<<grid_for(c, n, 256, 8), 256, 0, s>>>(c->r[src], c->id[src], n, c->split,
-                                                                       seg_table(c), B, cap, c->bcnt, nullptr,
-                                                                       nullptr, c->bidx, c->ctr);
+        const int64_t blocks = (n + 256 * kScatterItems - 1) / (256 * kScatterItems);
+        k_bucket_scatter_idx<<<(unsigned)blocks, 256, 0, s>>>(c->r[src], n, c->split, seg_table(c), c->tune.bshift,
+                                                               cap, c->bcnt, c->bidx, c->ctr);
         k_bucket_scan<<<1, 1024, 0, s>>>(c->bcnt, nb, cap, c->boff, c->ctr);
     }
     c->launches += 2;

@@ -1,6 +1,6 @@
 // nsg_fused.cuh -- the near-sorted sort done inside the kernel that consumes it.
 //
-// The scatter pass (k_bucket_scatter<true>, nsg_bucket.cu) leaves, for every bucket b
+// The scatter pass (k_bucket_scatter_idx, nsg_bucket.cu) leaves, for every bucket b
 // of the previous sort's splitters, the source indices of the particles whose key
 // falls in [S[b], S[b+1]) in bidx[b * cap ..].  One block per bucket then
 //   1. loads the indices, and through them r and id (coalesced in near-sorted order);

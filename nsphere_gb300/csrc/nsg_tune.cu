@@ -131,7 +131,8 @@ int nsg_autotune(nsg_ctx *c, int steps, char *report, int report_cap)
     std::string log = "{";
     char buf[256];
 
-    // score = profiled milliseconds of the named kernels over `steps` steps
+    // score = profiled milliseconds of the named kernels over `steps` steps (no
+    // names: every kernel but the Levi-Civita chains, which no knob here changes)
     auto trial = [&](const Tune &t, std::initializer_list<const char *> names, double &score) -> int {
         int32_t v[4] = {t.gl0_threads, t.gl0_bps, t.bshift, t.lanes_bps};
         if (int rc = nsg_tune_set(c, v, 4)) return rc;
@@ -144,9 +145,14 @@ int nsg_autotune(nsg_ctx *c, int steps, char *report, int report_cap)
         nsg_profile(c, 0);
         if (rc) return rc;
         score = 0.0;
-        for (int k = 0; k < cnt && k < 64; k++)
+        for (int k = 0; k < cnt && k < 64; k++) {
+            if (names.size() == 0) {
+                if (strcmp(st[k].name, "levi_civita") != 0 && strcmp(st[k].name, "lc_late") != 0)
+                    score += st[k].total_ms;
+            }
             for (const char *nm : names)
                 if (strcmp(st[k].name, nm) == 0) score += st[k].total_ms;
+        }
         return snap_put(c, snap);
     };
     auto fail = [&](int rc) {
@@ -160,28 +166,31 @@ int nsg_autotune(nsg_ctx *c, int steps, char *report, int report_cap)
 
     Tune best = orig;
     double s;
-    // 1. k_gather_level0 launch shape
-    const int shapes[][2] = {{128, 16}, {256, 8}, {256, 4}, {512, 4}, {512, 2}};
+    // 1. bucket target of the near-sorted sort (9..11: sorted inside the kernel that
+    //    consumes it; 12: bucket-sort kernel, then the gather), scored by the whole
+    //    step beside the chains
     double bests = 1e300;
-    log += "\"gather_level0\":[";
-    for (auto &sh : shapes) {
-        Tune t = best;
-        t.gl0_threads = sh[0]; t.gl0_bps = sh[1];
-        if (int rc = trial(t, {"gather_level0"}, s)) return fail(rc);
-        snprintf(buf, sizeof(buf), "%s[%d,%d,%.4f]", log.back() == '[' ? "" : ",", sh[0], sh[1], s / steps);
-        log += buf;
-        if (s < bests) { bests = s; best.gl0_threads = sh[0]; best.gl0_bps = sh[1]; }
-    }
-    // 2. bucket target of the near-sorted sort
-    bests = 1e300;
-    log += "],\"bucket_shift\":[";
-    for (int bs : {10, 11, 12}) {
+    log += "\"bucket_shift\":[";
+    for (int bs : {10, 9, 11, 12}) {
         Tune t = best;
         t.bshift = bs;
-        if (int rc = trial(t, {"bucket_scatter", "bucket_sort", "sort_radix", "sort_seed"}, s)) return fail(rc);
+        if (int rc = trial(t, {}, s)) return fail(rc);
         snprintf(buf, sizeof(buf), "%s[%d,%.4f]", log.back() == '[' ? "" : ",", bs, s / steps);
         log += buf;
         if (s < bests) { bests = s; best.bshift = bs; }
+    }
+    // 2. k_gather_level0 launch shape (the two-kernel path and the radix fallback's
+    //    consumer; the fused kernels have one block per bucket)
+    const int shapes[][2] = {{128, 16}, {256, 8}, {256, 4}, {512, 4}, {512, 2}};
+    bests = 1e300;
+    log += "],\"gather_level0\":[";
+    for (auto &sh : shapes) {
+        Tune t = best;
+        t.gl0_threads = sh[0]; t.gl0_bps = sh[1];
+        if (int rc = trial(t, {}, s)) return fail(rc);
+        snprintf(buf, sizeof(buf), "%s[%d,%d,%.4f]", log.back() == '[' ? "" : ",", sh[0], sh[1], s / steps);
+        log += buf;
+        if (s < bests) { bests = s; best.gl0_threads = sh[0]; best.gl0_bps = sh[1]; }
     }
     // 3. level-parallel kernel grid
     bests = 1e300;
@@ -189,7 +198,7 @@ int nsg_autotune(nsg_ctx *c, int steps, char *report, int report_cap)
     for (int lb : {2, 4, 8}) {
         Tune t = best;
         t.lanes_bps = lb;
-        if (int rc = trial(t, {"leap_levels"}, s)) return fail(rc);
+        if (int rc = trial(t, {}, s)) return fail(rc);
         snprintf(buf, sizeof(buf), "%s[%d,%.4f]", log.back() == '[' ? "" : ",", lb, s / steps);
         log += buf;
         if (s < bests) { bests = s; best.lanes_bps = lb; }

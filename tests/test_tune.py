@@ -30,7 +30,7 @@ def test_autotune_restores_state(nsg):
 def test_shapes_do_not_change_results(nsg):
     r, vr, ell, ids = ics.hernquist(40000, seed=32)
     out = []
-    for shape in [None, (128, 16, 10, 2), (512, 2, 12, 8), (256, 4, 8, 1)]:
+    for shape in [None, (128, 16, 10, 2), (512, 2, 12, 8), (256, 4, 8, 1), (256, 8, 9, 4), (256, 8, 11, 4)]:
         with nsg.Context(nsg.default_params(**KW)) as c:
             if shape is not None:
                 c.tune_set(shape)

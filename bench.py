@@ -43,14 +43,15 @@ UNIT = "particle-steps/s"
 # sort + scan + force pass, algorithmic bytes per particle: read r key 8, gather r v ell id 28,
 # write them 28, write the rank force 8
 SORT_PASS_BYTES = 72.0
-# DRAM bytes per particle of one k_gather_level0 launch (read + write), from an ncu capture
-# of that kernel at N = 5e6 (160.7 MB read + 121.8 MB written per launch)
-GATHER_LEVEL0_TRAFFIC = (160.67328e6 + 121.77024e6) / 5e6
+# DRAM bytes per particle of one k_fused_level0 launch (read + write), from an ncu capture
+# of that kernel on the Hernquist state at N = 5e6 (160.5 MB read + 113.2 MB written per
+# launch; traffic grows in proportion to N)
+FUSED_LEVEL0_TRAFFIC = (160.457216e6 + 113.236224e6) / 5e6
 # DRAM bytes of one k_levi_civita_pair launch, from an ncu capture of the Hernquist step
 # at N = 2e6 (62.7 KB read, nothing written back to DRAM during the launch); it does not
 # grow with N -- the launch touches only the Levi-Civita particles
 LC_TRAFFIC_PER_LAUNCH = 62.7e3
-# IEEE double operations per particle that k_gather_level0 issues at level 0
+# IEEE double operations per particle that the level-0 pass issues
 # (rank numerator 3, start force 5, coarse pass 9, fine pass 16, test 6, Richardson 6, l^2 1)
 LEVEL0_FLOPS = 46.0
 
@@ -58,7 +59,7 @@ LEVEL0_FLOPS = 46.0
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=10_000_000)
@@ -74,6 +75,9 @@ def parse():
     ap.add_argument("--post-runs", type=int, default=3,
                     help="timed runs of the snapshot post-processing of the final state (0: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch every step eagerly (for profilers that cannot see into graphs with "
+                         "conditional nodes); results are identical")
     return ap.parse_args()
 
 
@@ -136,6 +140,8 @@ def workload(args, seed_offset=0):
                    lc="adaptive levi-civita below r=1e-3", tol=1e-7, out_type=2)
         state = ics.hernquist(args.n, seed=replica_seed(2, seed_offset))
         params = dict(dt=dt_eq, max_subdiv=128, lc_rule=1, lc_radius=1e-3, method=5, max_tau_steps=1_000_000)
+    if args.no_graph:
+        params["graph"] = 0
     if args.dt is not None:
         # an explicit time step replaces the workload's (the point-mass ramp keeps its 500 steps)
         if "point_mass_rate" in params:
@@ -375,13 +381,15 @@ def main():
 
     # the sort + scan + force pass on its own: fixed-step leapfrog steps of the same
     # state (kick + drift, then bucket sort and the gather that writes the rank force)
-    kp = ns.default_params(dt=params["dt"], method=ns.METHOD_KDK)
+    kp = ns.default_params(dt=params["dt"], method=ns.METHOD_KDK, graph=params.get("graph", 1))
     ctx.set_params(kp)
     ctx.step(2)
+    ctx.clear_status()
     ctx.profile(True)
     ctx.step(nprof)
     kprof = ctx.profile_read()
     ctx.profile(False)
+    kdk_fallback = bool(ctx.status() & ns.ST_SORT_FALLBACK)
     ctx.set_params(p)
 
     # learned against plain schedule, and the energy drift of each over 1000 steps.
@@ -391,7 +399,11 @@ def main():
     # bit-identical states (the plain error test judges every particle), so their
     # |dE/E| are equal by construction and measured here over the whole run.
     learned = None
-    if args.workload in ("adaptive", "om") and args.ab_steps > 0 and sizes is None:
+    if args.workload in ("adaptive", "om", "stress") and args.ab_steps > 0 and sizes is None:
+        if args.workload == "stress":
+            # N = 1e8 at ~40 ms per step: a shorter comparison
+            args.ab_steps = min(args.ab_steps, 100)
+            args.train_steps = min(args.train_steps, 20)
         ctx.set_params(ns.default_params(**params))
         if args.workload == "adaptive":
             ctx.upload(r, vr, ell, ids)
@@ -522,16 +534,20 @@ def main():
         tot = sum(k["total_ms"] for k in prof) or 1.0
         lat = fp64["latency_cycles"]
         bulk = None
-        if "gather_level0" in by:
-            g = by["gather_level0"]
+        l0name = "fused_level0" if "fused_level0" in by else "gather_level0"
+        if l0name in by:
+            g = by[l0name]
             per = g["total_ms"] / g["launches"]
             ach = (g["bytes"] / g["launches"]) / (per / 1e3) / 1e9
             flops = LEVEL0_FLOPS * n / (per / 1e3) / 1e12
-            bulk = {"bound": "hbm", "kernel": "k_gather_level0", "achieved": ach, "peak": hbm_peak,
-                    "unit": "GB/s", "frac": ach / hbm_peak, "traffic": GATHER_LEVEL0_TRAFFIC * n,
-                    "peak_source": peak_src,
-                    "note": "the largest kernel beside the chains; compute-bound on the FP64 pipe "
-                            "(ncu: 82% FP64 pipe active); FP64 view below",
+            bulk = {"bound": "hbm", "kernel": "k_" + l0name, "achieved": ach, "peak": hbm_peak,
+                    "unit": "GB/s", "frac": ach / hbm_peak,
+                    "traffic": (FUSED_LEVEL0_TRAFFIC * n) if (FUSED_LEVEL0_TRAFFIC and l0name == "fused_level0")
+                    else None,
+                    "peak_source": peak_src, "ms": per,
+                    "note": "the sort of the step (in shared memory) and adaptive level 0 in one kernel; "
+                            "65 algorithmic bytes per particle; bound by the FP64 pipe (46 IEEE operations "
+                            "per particle at level 0); FP64 view below",
                     "fp64": {"achieved_tflops": flops, "peak_tflops": fp64["dfma_tflops"],
                              "frac": flops / fp64["dfma_tflops"],
                              "peak_source": "measured live by nsg_probe_fp64 (FMA = 2 flops)"}}
@@ -540,6 +556,7 @@ def main():
         # writes r, v_r and its level (17 B).
         roof = None
         lcs = by.get("levi_civita")
+        roof_lc = None
         if lcs:
             per = lcs["total_ms"] / lcs["launches"]
             alg = 49.0 * n_lc
@@ -551,17 +568,30 @@ def main():
                             "chain of dependent FP64 operations; its bound is the dependent latency, "
                             "latency_frac = floor / measured cycles per substep",
                     "latency_frac": (9 * lat["fp64_fma"] + lat["div_latency_form"]) / lat["levi_civita_substep"]}
-        sort_names = ["bucket_scatter", "bucket_sort", "sort_seed", "sort_radix", "gather_kick"]
+            roof_lc = dict(roof)
+        # The pass of a fixed-step leapfrog step: index scatter + bucket scan, then the
+        # fused sort + rank force + kick.  The radix fallback's kernels (launched eagerly
+        # here, returning at once; skipped by the conditional graph node of a replayed
+        # step) count only when the fallback ran.
+        if "fused_kick" in kby:
+            sort_names = ["bucket_scatter", "fused_kick"]
+            if kdk_fallback:
+                sort_names += ["sort_seed", "sort_radix", "gather_kick_fallback"]
+        else:
+            sort_names = ["bucket_scatter", "bucket_sort", "sort_seed", "sort_radix", "gather_kick"]
         sort_ms = sum(kby[k]["total_ms"] for k in sort_names if k in kby) / nprof
         sort_gbs = SORT_PASS_BYTES * n / (sort_ms / 1e3) / 1e9 if sort_ms else None
+        # the roofline object names the kernel with the largest share of the timed steps
+        top = max(prof, key=lambda k: k["total_ms"]) if prof else None
+        if top is not None and top["name"] == l0name and bulk is not None:
+            roof = dict(bulk)
         if roof is None and sort_gbs:
             # no Levi-Civita chains (fixed-step leapfrog): the sort + scan + force pass dominates
-            roof = {"bound": "hbm", "kernel": "sort + scan + force pass (k_bucket_scatter, k_bucket_sort, "
-                                              "k_gather_rank_force)",
+            roof = {"bound": "hbm", "kernel": "sort + scan + force pass (k_bucket_scatter_idx, k_bucket_scan, "
+                                              "k_fused_rank_force)",
                     "achieved": sort_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": sort_gbs / hbm_peak,
                     "traffic": None, "peak_source": peak_src,
-                    "note": "72 algorithmic bytes per particle; the in-bucket sort is shared-memory and "
-                            "issue bound, the gather FP64-pipe bound"}
+                    "note": "72 algorithmic bytes per particle"}
         lc = by.get("levi_civita")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -590,7 +620,10 @@ def main():
             "sort_scan_force": {"ms": sort_ms, "GBps": sort_gbs,
                                 "frac": (sort_gbs / hbm_peak) if sort_gbs else None,
                                 "bytes_per_particle": SORT_PASS_BYTES,
-                                "kernels": [k for k in sort_names if k in kby]},
+                                "kernels": {k: kby[k]["total_ms"] / nprof for k in sort_names if k in kby},
+                                "radix_fallback_ran": kdk_fallback,
+                                "workload": "fixed-step leapfrog steps of the timed state"},
+            "lc_roofline": roof_lc,
             "kernels": [{"name": k["name"], "ms_per_step": k["total_ms"] / nprof, "share": k["total_ms"] / tot}
                         for k in prof],
             "fp64_probe": fp64,

@@ -276,6 +276,7 @@ static void free_buffers(nsg_ctx *c)
     f(c->d_seg_start); f(c->d_bbase); f(c->seg_energy);
     c->nb_cap = 0;
     c->bidx_cap = 0;
+    c->bslot_cap = 0;
     c->cap = 0;
 }
 
@@ -549,14 +550,21 @@ static int setup_segments(nsg_ctx *c, const int64_t *seg_n, int nseg)
     auto F = [](auto *&p) { if (p) cudaFree((void *)p); p = nullptr; };
     cudaError_t e = cudaSuccess;
     if (nb > c->nb_cap) {
-        F(c->split); F(c->bcnt); F(c->boff); F(c->bkey); F(c->bpay);
+        F(c->split); F(c->bcnt); F(c->boff);
         e = cudaMalloc((void **)&c->split, (size_t)nb * 8);
         if (e == cudaSuccess) e = cudaMalloc((void **)&c->bcnt, (size_t)nb * 4);
         if (e == cudaSuccess) e = cudaMalloc((void **)&c->boff, (size_t)nb * 4);
-        if (e == cudaSuccess) e = cudaMalloc((void **)&c->bkey, (size_t)nb * kBucketCap * 8);
-        if (e == cudaSuccess) e = cudaMalloc((void **)&c->bpay, (size_t)nb * kBucketCap * 8);
         if (e != cudaSuccess) return cuda_err(c, e, "bucket buffers");
         c->nb_cap = nb;
+    }
+    const int64_t nbs = nb * (int64_t)bucket_cap(c);
+    if (nbs > c->bslot_cap) {
+        F(c->bkey); F(c->bpay);
+        c->bslot_cap = 0;
+        e = cudaMalloc((void **)&c->bkey, (size_t)nbs * 8);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&c->bpay, (size_t)nbs * 8);
+        if (e != cudaSuccess) return cuda_err(c, e, "bucket slot buffers");
+        c->bslot_cap = nbs;
     }
     const int64_t nbi = nb * (int64_t)fused_cap(c);
     if (nbi > c->bidx_cap) {

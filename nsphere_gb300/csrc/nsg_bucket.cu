@@ -121,8 +121,8 @@ k_bucket_scatter_idx(const double *__restrict__ r, int64_t n, const uint64_t *__
         int b = -1;
         if (valid) {
             const double rp = rv[j];
-            nan_seen |= (rp != rp);
             const uint64_t key = radius_key(rp);
+            nan_seen |= (key == ~0ull);          // NaN, tested on the integer pipe
             const Local L = local_of(sg, p, n);
             const int lo = sg.bbase[L.h], hi = sg.bbase[L.h + 1];
             int home = lo + (int)(L.i >> bshift);
@@ -469,13 +469,22 @@ size_t bucket_smem_bytes(int cap)
     return (size_t)cap * 8 + (size_t)kBucketWarps * 256 * 4 + 256 * 4;
 }
 
+// Slot capacity of a bucket on the two-kernel path: three times the bucket target,
+// rounded up to whole 1024-thread rows of k_bucket_sort (which writes its padding
+// items too), at most kBucketCap.
+int bucket_cap(const nsg_ctx *c)
+{
+    const int want = ((3 << c->tune.bshift) + 1023) & ~1023;
+    return want < kBucketCap ? want : kBucketCap;
+}
+
 // Fast path of the sort.  Returns NSG_OK having launched the bucket kernels; the
 // radix kernels that follow run only if the scan flagged an overflow.
 int bucket_sort_perm(nsg_ctx *c)
 {
     const int64_t n = c->n;
     const int src = c->cur;
-    const int B = 1 << c->tune.bshift, cap = kBucketCap;
+    const int B = 1 << c->tune.bshift, cap = bucket_cap(c);
     const int nb = (int)c->nb_total;
     cudaStream_t s = c->stream;
     cudaError_t e = cudaMemsetAsync(c->bcnt, 0, (size_t)nb * 4, s);

@@ -113,7 +113,8 @@ struct nsg_ctx {
     uint64_t *split = nullptr;       // [nb_total] splitter keys from the last sort
     bool split_valid = false;
     unsigned int *bcnt = nullptr, *boff = nullptr;  // [nb]
-    uint64_t *bkey = nullptr, *bpay = nullptr;      // [nb * kBucketCap]
+    uint64_t *bkey = nullptr, *bpay = nullptr;      // [nb * bucket_cap] (two-kernel path)
+    int64_t bslot_cap = 0;                          // entries allocated in bkey, bpay
     uint32_t *bidx = nullptr;                       // [nb * fused_cap] (fused path)
     int64_t bidx_cap = 0;                           // entries allocated in bidx
 
@@ -408,6 +409,7 @@ int kdk_first_half(nsg_ctx *c);                       // kick (a0 of the current
 int compute_energy(nsg_ctx *c);                       // K, W of the sorted live copy
 int bucket_sort_perm(nsg_ctx *c);                     // near-sorted fast path (sets need_fallback)
 int fused_cap(const nsg_ctx *c);                      // entries of a fused sort block (0: fused path off)
+int bucket_cap(const nsg_ctx *c);                     // slots per bucket of the two-kernel path
 int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s); // scatter indices + scan for the fused kernels
 bool use_fused(const nsg_ctx *c);                     // the sort of this step runs inside its consumer
 // Launches the radix sort and then `tail` on stream s so that they run only when

@@ -77,18 +77,18 @@ struct StepArgs {
 // Micro leapfrog, nsphere.c:1550-1607: half-kick, (pairs-1) drift-kick pairs, drift,
 // half-kick.  pairs = N (coarse, 2N+1 substeps) or 2N (fine, 4N+1 substeps); the
 // first acceleration a_first = acc(r_in) is passed in.
-template <bool HW>
+template <bool HW, bool EM = false>
 __device__ __forceinline__ void micro_leap(double r, double v, double l2, double gn,
                                            double hk, double ms, int64_t pairs, double a_first,
                                            double &r_out, double &v_out)
 {
-    v = dadd(v, dmul(hk, a_first));
+    v = dadd(v, tmul<EM>(hk, a_first));
     for (int64_t pp = 1; pp <= pairs - 1; pp++) {
-        r = dadd(r, dmul(ms, v));
-        v = dadd(v, dmul(ms, acc_leap<HW>(r, gn, l2)));
+        r = dadd(r, tmul<EM>(ms, v));
+        v = dadd(v, tmul<EM>(ms, acc_leap<HW, EM>(r, gn, l2)));
     }
-    r = dadd(r, dmul(ms, v));
-    v = dadd(v, dmul(hk, acc_leap<HW>(r, gn, l2)));
+    r = dadd(r, tmul<EM>(ms, v));
+    v = dadd(v, tmul<EM>(hk, acc_leap<HW, EM>(r, gn, l2)));
     r_out = r;
     v_out = v;
 }
@@ -112,14 +112,15 @@ __device__ __forceinline__ bool converged(double rc, double vc, double rf, doubl
     return ok_r && ok_v;
 }
 
+template <bool EM = false>
 __device__ __forceinline__ void select_out(int out_type, double rc, double vc, double rf,
                                            double vf, double &ro, double &vo)
 {
     if (out_type == 0) { ro = rc; vo = vc; }
     else if (out_type == 1) { ro = rf; vo = vf; }
     else {
-        ro = dsub(mul4(rf), dmul(3.0, rc));
-        vo = dsub(mul4(vf), dmul(3.0, vc));
+        ro = dsub(mul4(rf), tmul<EM>(3.0, rc));
+        vo = dsub(mul4(vf), tmul<EM>(3.0, vc));
     }
 }
 
@@ -176,8 +177,13 @@ __device__ __forceinline__ void level0_particle(const StepArgs &a, int64_t i, co
         }
         return;
     }
+    // The pass is bound by the FP64 pipe, and the integer pipes already carry its
+    // divisions and the sort: the coarse pass's, ell^2's and the Richardson step's
+    // multiplications (8 of 19) run on the integer pipes, the rest on the FP64 pipe
+    // (all 19 on the integer pipes measured slower than none).
+    constexpr bool EM = true;
     const double gn = gnum_of(L.i, L.n, a.G, a.M, Mpt);
-    const double l2 = dmul(ell, ell);
+    const double l2 = tmul<EM>(ell, ell);
     const double af = acc_leap(r, gn, l2);
     // learned schedule: a particle predicted to need level >= 1 goes straight to
     // the level-parallel kernel, which tests every level from 0 upward
@@ -185,14 +191,14 @@ __device__ __forceinline__ void level0_particle(const StepArgs &a, int64_t i, co
     double rc = 0.0, vc = 0.0, rf = 0.0, vf = 0.0;
     bool done = false;
     if (!fresh) {
-        micro_leap<false>(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
+        micro_leap<false, EM>(r, v, l2, gn, a.hk_c0, a.ms_c0, 1, af, rc, vc);
         micro_leap<false>(r, v, l2, gn, a.hk_f[0], a.ms_f[0], 2, af, rf, vf);
         const bool ok = converged<false>(rc, vc, rf, vf, rf, a);
         const bool bad = !(finite_bits(rf) && finite_bits(vf));
         done = ok || last || (bad && a.nf_stop);
         if (done) {
             double ro, vo;
-            select_out(a.out_type, rc, vc, rf, vf, ro, vo);
+            select_out<EM>(a.out_type, rc, vc, rf, vf, ro, vo);
             a.r_out[i] = ro;
             a.v_out[i] = vo;
             a.level[i] = ok ? 0 : kLevelNotConverged;
@@ -1072,9 +1078,9 @@ k_kick_drift(double *__restrict__ r, double *__restrict__ v, const double *__res
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        double vi = dadd(v[i], dmul(half_exact(a0[i]), dt));
+        double vi = dadd(v[i], mul_rn(half_exact(a0[i]), dt));
         v[i] = vi;
-        r[i] = dadd(r[i], dmul(vi, dt));
+        r[i] = dadd(r[i], mul_rn(vi, dt));
     }
 }
 

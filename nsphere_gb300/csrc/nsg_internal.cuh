@@ -8,6 +8,7 @@
 
 #include "nsg.h"
 #include "nsg_div.cuh"
+#include "nsg_mul.cuh"
 
 namespace nsg {
 
@@ -301,12 +302,19 @@ __device__ __forceinline__ double half_exact(double x)
     return dmul_call(0.5, x);
 }
 
+// Multiplication of the throughput kernels: EM = on the integer pipes (mul_rn,
+// nsg_mul.cuh), else on the FP64 pipe.  Both are IEEE round-to-nearest, so the choice
+// never changes a bit; kernels bound by the FP64 pipe move their products off it,
+// serial chains (bound by latency) keep the FP64 pipe's.
+template <bool EM>
+__device__ __forceinline__ double tmul(double a, double b) { return EM ? mul_rn(a, b) : dmul(a, b); }
+
 // gravity + centrifugal: gnum/(r*r) + l2/(r*r*r), nsphere.c:502-535.
-template <bool HW = false>
+template <bool HW = false, bool EM = false>
 __device__ __forceinline__ double acc_leap(double r, double gnum, double l2)
 {
-    double r2 = dmul(r, r);
-    return dadd(ddivx<HW>(gnum, r2), ddivx<HW>(l2, dmul(r2, r)));
+    double r2 = tmul<EM>(r, r);
+    return dadd(ddivx<HW>(gnum, r2), ddivx<HW>(l2, tmul<EM>(r2, r)));
 }
 
 // Order-preserving map of a double to uint64: -0.0 -> +0.0, NaN -> all ones.

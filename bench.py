@@ -463,10 +463,17 @@ def main():
         ctx.set_params(p)
         ctx.upload(r, vr, ell, ids)
 
-    # end to end through the public C ABI with host buffers: upload (pinned), step, download
+    # End to end through the public C ABI with host buffers, as a driver whose state
+    # lives on the host (the reference's loop) runs it: every step uploads the host
+    # state (pinned), steps once and reads the result back into the host state the
+    # next step uploads.  The host state starts as the state after two steps of the
+    # context's current state (in the order of a sort, as a driver's state is after
+    # its first step).
     pin = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(8)]
-    h_r, h_v, h_l, h_i, o_r, o_v, o_l, o_i = [t.numpy() for t in pin]
-    h_r[:], h_v[:], h_l[:], h_i[:] = r, vr, ell, ids
+    bufs = [[t.numpy() for t in pin[:4]], [t.numpy() for t in pin[4:]]]
+    ctx.step(2)
+    for dst, src in zip(bufs[0], ctx.download()):
+        dst[:] = src
     lib = ns.lib()
 
     def P(a):
@@ -476,7 +483,9 @@ def main():
     ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ee0.record(stream)
     hn = None if sizes is None else np.ascontiguousarray(sizes, dtype=np.int64)
-    for _ in range(args.e2e_steps):
+    for k in range(args.e2e_steps):
+        h_r, h_v, h_l, h_i = bufs[k & 1]
+        o_r, o_v, o_l, o_i = bufs[(k + 1) & 1]
         if hn is None:
             ctx._check(lib.nsg_upload(ctx.handle, P(h_r), P(h_v), P(h_l), P(h_i), None, n))
         else:

@@ -592,6 +592,14 @@ static int upload_common(nsg_ctx *c, int64_t n, const int64_t *seg_n = nullptr, 
     if (n <= 0 || n > (int64_t)0x7fffffff) return set_err(c, NSG_EINVAL, "n must be in [1, 2^31-1]");
     if (nseg < 1 || nseg > 65536) return set_err(c, NSG_EINVAL, "1 to 65536 halos");
     drop_graph(c);
+    // A driver that uploads every step (the reference's loop keeps its state on the
+    // host) uploads a state close to the last sort's order: the splitters of that sort
+    // stay usable when the halo table is the same.  Any non-decreasing splitters give a
+    // correct sort -- an unrelated state only overflows buckets and takes the radix
+    // fallback -- so keeping them is safe.
+    const std::vector<int64_t> old_start = c->h_seg_start;
+    const int64_t old_nb = c->nb_total;
+    const bool old_split = c->split_valid && c->n == n;
     if (int rc = ensure_capacity(c, n)) return rc;
     c->n = n;
     const int64_t one = n;
@@ -599,7 +607,7 @@ static int upload_common(nsg_ctx *c, int64_t n, const int64_t *seg_n = nullptr, 
     c->cur = 0;
     c->sorted = false;
     c->inv_valid = false;
-    c->split_valid = false;
+    c->split_valid = old_split && old_start == c->h_seg_start && old_nb == c->nb_total;
     return NSG_OK;
 }
 

@@ -472,3 +472,40 @@ def test_step_download_carries_aux(nsg):
                 outs.append(c.download(with_aux=True))
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
+
+
+def test_reupload_keeps_splitters_and_results(nsg, oracle):
+    """A driver that uploads its host state every step: the previous sort's splitters
+    stay in use when the halo table is unchanged.  Re-uploading the downloaded state
+    continues bit for bit like uninterrupted steps.  The buckets are key ranges, so a
+    shuffled state of the same distribution sorts through them as well; a state whose
+    radii lie elsewhere overflows them and the radix sort takes over.  Both are exact."""
+    n = 60_000
+    r, vr, ell, ids = _adaptive_case(n, 61, lowl=150)
+    kw = dict(dt=1e-3, max_subdiv=64, lc_rule=1, lc_radius=5e-2)
+    p = oracle.params(**kw)
+    cur = (r, vr, ell, ids)
+    for _ in range(5):
+        cur = oracle.step_adaptive(p, *cur)[:4]
+    with _ctx(nsg, **kw) as c:
+        c.upload(r, vr, ell, ids)
+        c.step(2)
+        mid = c.download()
+        for _ in range(3):
+            c.upload(*mid)
+            c.step(1)
+            mid = c.download()
+        for g, o in zip(mid, cur):
+            assert np.array_equal(g, o)
+        # unrelated states of the same size: shuffled, same distribution; then radii
+        # twenty times larger (all above the old splitters but the last few)
+        r2, v2, l2, i2 = _shuffle(7, *_adaptive_case(n, 62, lowl=0))
+        for scale, fallback in ((1.0, False), (20.0, True)):
+            c.clear_status()
+            c.upload(r2 * scale, v2, l2, i2)
+            c.sort()
+            got = c.download()
+            assert bool(c.status() & nsg.ST_SORT_FALLBACK) == fallback
+            want = oracle.sort(r2 * scale, v2, l2, i2)
+            for g, o in zip(got, want):
+                assert np.array_equal(g, o)

@@ -296,8 +296,14 @@ NSG_HD double div_rn_lat(double a, double b, bool &ok)
 #if defined(__CUDACC__)
 // The FP64 pipe's division behind a call: the compiler cannot predicate or hoist the
 // division's instructions into the caller, so they run only for the operands the
-// integer forms leave (a predicated inline fallback halves the throughput).
-static __device__ __noinline__ double div_rn_slow(double a, double b) { return __ddiv_rn(a, b); }
+// integer forms leave (a predicated inline fallback halves the throughput).  The
+// operands cross the call as bit patterns: passed as doubles, the call costs the caller
+// one FP64-pipe instruction on every division, taken or not (measured with the pipe
+// counters), which the throughput kernels, bound by that pipe, cannot spare.
+static __device__ __noinline__ double div_rn_slow(unsigned long long ua, unsigned long long ub)
+{
+    return __ddiv_rn(__longlong_as_double((long long)ua), __longlong_as_double((long long)ub));
+}
 
 // Correctly rounded a / b (round to nearest even), bit-identical to __ddiv_rn: the
 // latency form, whose few integer and FP32 steps also give the highest throughput
@@ -306,7 +312,7 @@ __device__ __forceinline__ double div_rn(double a, double b)
 {
     bool ok;
     double q = div_rn_lat(a, b, ok);
-    if (!ok) q = div_rn_slow(a, b);
+    if (!ok) q = div_rn_slow(div_bits(a), div_bits(b));
     return q;
 }
 

@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(512) k_gather_level0(StepArgs a)
 // bucket b and does the level-0 work of its sorted positions off[b] ..; the sort's
 // integer and shared-memory work overlaps other blocks' FP64 work on the same SM.
 template <bool AUX, int T>
-__global__ void __launch_bounds__(T, T == 128 ? 6 : (T == 256 ? 3 : 1)) k_fused_level0(StepArgs a, FusedSort fs)
+__global__ void __launch_bounds__(T, T == 128 ? 6 : (T == 256 ? 4 : 1)) k_fused_level0(StepArgs a, FusedSort fs)
 {
     if (a.ctr->need_fallback) return;
     const int b = blockIdx.x;

@@ -191,9 +191,25 @@ __device__ __forceinline__ bool open_between(double r, double lo, double hi)
 // Rare operand paths behind calls.  A branch whose other side issues FP64
 // instructions is if-converted by the compiler -- both sides are computed and one is
 // selected -- so an inline slow path costs its FP64 issue slots on every call; a call
-// cannot be predicated that way, so its instructions run only when it is taken.
-static __device__ __noinline__ double dmul_call(double a, double b) { return __dmul_rn(a, b); }
-static __device__ __noinline__ double dadd_call(double a, double b) { return __dadd_rn(a, b); }
+// cannot be predicated that way, so its instructions run only when it is taken.  The
+// operands cross the call as bit patterns (a double argument costs an FP64-pipe
+// instruction at every call site, taken or not).
+static __device__ __noinline__ double dmul_call_bits(unsigned long long a, unsigned long long b)
+{
+    return __dmul_rn(__longlong_as_double((long long)a), __longlong_as_double((long long)b));
+}
+static __device__ __noinline__ double dadd_call_bits(unsigned long long a, unsigned long long b)
+{
+    return __dadd_rn(__longlong_as_double((long long)a), __longlong_as_double((long long)b));
+}
+__device__ __forceinline__ double dmul_call(double a, double b)
+{
+    return dmul_call_bits((unsigned long long)dbits(a), (unsigned long long)dbits(b));
+}
+__device__ __forceinline__ double dadd_call(double a, double b)
+{
+    return dadd_call_bits((unsigned long long)dbits(a), (unsigned long long)dbits(b));
+}
 
 // x + 1e-30 for x >= +0 or NaN.  From x = 2^-46 up, 1e-30 is below half an ulp of x
 // (2^-99), so the sum rounds to x; only smaller x take the FP64 addition.
@@ -276,8 +292,11 @@ __device__ __forceinline__ double ddiv(double a, double b) { return div_rn(a, b)
 // G = M = 1 (the units of the benchmark halos) both products are exact: the result
 // is the quotient with its sign flipped, and no FP64 instruction is issued (the
 // tests of G, M and Mpt compare bit patterns on the integer pipe).
-static __device__ __noinline__ double gnum_general(double q, double G, double M, double Mpt)
+static __device__ __noinline__ double gnum_general(unsigned long long qb, unsigned long long Gb, unsigned long long Mb,
+                                                   unsigned long long Mptb)
 {
+    const double q = __longlong_as_double((long long)qb), G = __longlong_as_double((long long)Gb);
+    const double M = __longlong_as_double((long long)Mb), Mpt = __longlong_as_double((long long)Mptb);
     double g = __dmul_rn(__dmul_rn(-G, q), M);
     if (Mpt != 0.0) g = __dsub_rn(g, __dmul_rn(G, Mpt));
     return g;
@@ -290,7 +309,8 @@ __device__ __forceinline__ double gnum_of(int64_t i, int64_t n, double G, double
     constexpr long long kOne = 0x3ff0000000000000ll;
     if (dbits(G) == kOne && dbits(M) == kOne && (dbits(Mpt) << 1) == 0)   // Mpt == 0.0
         return __longlong_as_double(dbits(q) ^ (long long)0x8000000000000000ull);
-    return gnum_general(q, G, M, Mpt);
+    return gnum_general((unsigned long long)dbits(q), (unsigned long long)dbits(G), (unsigned long long)dbits(M),
+                        (unsigned long long)dbits(Mpt));
 }
 
 // 0.5 x: for a normal x whose half stays normal the exponent field falls by one

@@ -49,13 +49,17 @@ NSG_HD double mul_rn_int(double a, double b, bool &ok)
 // Correctly rounded a * b, bit-identical to __dmul_rn: the integer form, with the FP64
 // pipe's multiplication behind a call for the operands it declines (a call cannot be
 // if-converted, so the FP64 instruction issues only when it is needed).
-static __device__ __noinline__ double mul_rn_slow(double a, double b) { return __dmul_rn(a, b); }
+// (Operands cross the call as bit patterns, as for div_rn_slow.)
+static __device__ __noinline__ double mul_rn_slow(unsigned long long ua, unsigned long long ub)
+{
+    return __dmul_rn(__longlong_as_double((long long)ua), __longlong_as_double((long long)ub));
+}
 
 __device__ __forceinline__ double mul_rn(double a, double b)
 {
     bool ok;
     double q = mul_rn_int(a, b, ok);
-    if (!ok) q = mul_rn_slow(a, b);
+    if (!ok) q = mul_rn_slow(div_bits(a), div_bits(b));
     return q;
 }
 #endif

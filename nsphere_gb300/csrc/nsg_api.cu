@@ -2,6 +2,7 @@
 // context lifetime, device buffers, host <-> device transfer, step orchestration,
 // diagnostics and profiling.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <chrono>
 #include <thread>
@@ -436,7 +437,12 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_lcsel, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->body, cudaStreamNonBlocking);
-    if (e == cudaSuccess) c->cond_nodes = cond_nodes_supported();
+    // NSG_NO_CONDITIONAL_NODES=1 takes the path of drivers without conditional nodes
+    // (the radix fallback launched directly inside a captured step), for tests
+    if (e == cudaSuccess) {
+        const char *nc = getenv("NSG_NO_CONDITIONAL_NODES");
+        c->cond_nodes = cond_nodes_supported() && !(nc && nc[0] == '1');
+    }
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->ctr, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMemset(c->ctr, 0, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_ctr, sizeof(DevCounters));

@@ -46,12 +46,17 @@ def test_graph_replay_ensemble(nsg):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("cond", [1, 0], ids=["conditional_node", "direct"])
 @pytest.mark.parametrize("method", [2, 5])
-def test_graph_replay_with_radix_fallback(nsg, method):
+def test_graph_replay_with_radix_fallback(nsg, method, cond, monkeypatch):
     """10000 particles at rest at r = 1 without gravity keep equal radii, so every
     near-sorted sort overflows its bucket and the radix sort runs: in a replayed graph
-    it sits in a conditional node that the overflow opens.  Replay equals eager launches,
-    and the equal radii stay ordered by id."""
+    it sits in a conditional node that the overflow opens (or, where the driver builds
+    no conditional nodes -- forced here by NSG_NO_CONDITIONAL_NODES -- its kernels are
+    captured directly and return at once when not needed).  Replay equals eager
+    launches either way, and the equal radii stay ordered by id."""
+    if not cond:
+        monkeypatch.setenv("NSG_NO_CONDITIONAL_NODES", "1")
     rng = np.random.default_rng(8)
     n, ntie = 30000, 10000
     r = rng.uniform(0.1, 3.0, n)

@@ -80,14 +80,32 @@ __device__ __forceinline__ void load_bT(const __nv_bfloat16 *W, int ld, int k0, 
 }
 
 // Features of one particle (FP32), nsg_mlp.cu header.
-__device__ __forceinline__ void mlp_features(double r, double v, double ell, double gn, double dt, float f[4])
+// x as a float, its significand truncated, built from the double's bits on the integer
+// pipe (a conversion instruction would issue to the FP64 pipe, which the step's
+// kernels saturate; the features need a few bits only): magnitudes above the float
+// range give infinity, below it zero; NaN gives infinity.
+__device__ __forceinline__ float f32_trunc(double x)
 {
-    const float rf = fmaxf((float)r, 1e-30f);
-    const float vc = sqrtf(fmaxf(-(float)gn / rf, 1e-30f));
+    const unsigned long long u = (unsigned long long)dbits(x);
+    const uint32_t sign = (uint32_t)(u >> 63) << 31;
+    const int e = (int)((u >> 52) & 0x7ffu) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((uint32_t)e << 23) | (uint32_t)((u >> 29) & 0x7fffffu));
+}
+
+// Features of one particle in FP32: log r, v_r over the circular speed, log of ell over
+// r times it, log of dt over the local dynamical time r / v_c, with v_c^2 = -gn / r
+// from the rank force numerator gn (also in FP32: the features steer only which
+// level is tried first, never a result).
+__device__ __forceinline__ void mlp_features(double r, double v, double ell, float gnf, float dtf, float f[4])
+{
+    const float rf = fmaxf(f32_trunc(r), 1e-30f);
+    const float vc = sqrtf(fmaxf(-gnf / rf, 1e-30f));
     f[0] = log2f(rf) * 0.125f;
-    f[1] = fminf(fmaxf((float)v / vc, -8.f), 8.f) * 0.25f;
-    f[2] = log2f(fabsf((float)ell) / (rf * vc) + 1e-6f) * 0.125f;
-    f[3] = log2f((float)dt * vc / rf + 1e-30f) * 0.125f;
+    f[1] = fminf(fmaxf(f32_trunc(v) / vc, -8.f), 8.f) * 0.25f;
+    f[2] = log2f(fabsf(f32_trunc(ell)) / (rf * vc) + 1e-6f) * 0.125f;
+    f[3] = log2f(dtf * vc / rf + 1e-30f) * 0.125f;
 }
 
 // Forward pass of one 16-row tile held by a warp.  x: this thread's rows g and g+8,
@@ -221,7 +239,8 @@ __global__ void __launch_bounds__(256) k_mlp_features(MlpStepArgs s, MlpDev m)
     __shared__ __nv_bfloat16 sW[kParams];
     __shared__ float sB[kBias];
     if (PREDICT) mlp_stage(m, sW, sB);
-    const double Mpt = s.ctr->point_mass;
+    const float Gf = f32_trunc(s.G), Mf = f32_trunc(s.M), Mptf = f32_trunc(s.ctr->point_mass);
+    const float dtf = f32_trunc(s.dt);
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -231,8 +250,8 @@ __global__ void __launch_bounds__(256) k_mlp_features(MlpStepArgs s, MlpDev m)
         if (i < s.n) {
             const uint32_t src = s.perm[i];
             const Local L = local_of(s.seg, i, s.n);
-            const double gn = gnum_of(L.i, L.n, s.G, s.M, Mpt);
-            mlp_features(s.r_src[src], s.v_src[src], s.l_src[src], gn, s.dt, f);
+            const float gnf = -Gf * ((float)(int32_t)L.i / (float)(int32_t)L.n) * Mf - Gf * Mptf;
+            mlp_features(s.r_src[src], s.v_src[src], s.l_src[src], gnf, dtf, f);
             if (!PREDICT)
                 for (int q = 0; q < 4; q++) m.feat[i * 4 + q] = f[q];
         }

@@ -355,17 +355,33 @@ def test_large_sort_properties(nsg):
     assert np.array_equal(sv, vr[src[sid]]) and np.array_equal(sl, ell[src[sid]])
 
 
-def test_large_step_energy_drift(nsg):
-    """N = 1e6 Hernquist, 20 adaptive steps: relative energy drift stays small."""
+@pytest.mark.parametrize("dt, bound", [(5e-4, 3e-6), (4e-5, 2e-8)])
+def test_energy_drift_matches_oracle_n1e6(nsg, oracle, dt, bound):
+    """N = 1e6 Hernquist, 20 adaptive steps: the state equals the oracle's bit for bit,
+    so its drift is the oracle's; the drift grows as dt^2 per step (about 1e-7 per step
+    at dt = 5e-4, 6e-10 at the bench's 4e-5), and stays within that bound."""
     n = 1_000_000
     r, vr, ell, ids = ics.hernquist(n, seed=2)
-    with _ctx(nsg, dt=5e-4, max_subdiv=128, lc_rule=1, lc_radius=1e-3) as c:
+    kw = dict(dt=dt, max_subdiv=128, lc_rule=1, lc_radius=1e-3)
+    with _ctx(nsg, **kw) as c:
         c.upload(r, vr, ell, ids)
         E0 = sum(c.energy())
         c.step(20)
+        gpu = c.download()
         E1 = sum(c.energy())
         st = c.status()
-    assert abs(E1 - E0) / abs(E0) < 1e-4
+    p = oracle.params(**kw)
+    cur = (r, vr, ell, ids)
+    for _ in range(20):
+        cur = oracle.step_adaptive(p, *cur)[:4]
+    for g, o in zip(gpu, cur):
+        assert np.array_equal(g, o)
+    srt = oracle.sort(*cur)
+    s0 = oracle.sort(r, vr, ell, ids)
+    e0 = sum(oracle.energy(p, s0[0], s0[1], s0[2]))
+    e1 = sum(oracle.energy(p, srt[0], srt[1], srt[2]))
+    assert abs(abs(E1 - E0) / abs(E0) - abs(e1 - e0) / abs(e0)) <= 2e-12
+    assert abs(E1 - E0) / abs(E0) < bound
     assert not (st & nsg.ST_TAU_CAP)
 
 

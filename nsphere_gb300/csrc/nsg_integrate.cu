@@ -1190,9 +1190,10 @@ static int level0_tail(nsg_ctx *c, cudaStream_t st, const unsigned *run_if, void
 
 // The fused sort + level 0 on stream st: index scatter and scan, one block per
 // bucket, then the radix fallback with its two-kernel consumers.
-static int fused_level0(nsg_ctx *c, StepArgs &a, cudaStream_t st, bool select)
+static int fused_level0(nsg_ctx *c, StepArgs &a, cudaStream_t st, bool select, bool prepared = false)
 {
-    if (int rc = bucket_fused_prepare(c, st)) return rc;
+    if (!prepared)
+        if (int rc = bucket_fused_prepare(c, st)) return rc;
     a.perm = a.perm_w = c->vals[0];   // the radix fallback's even pass count ends in vals[0] too
     const int cap = fused_cap(c);
     const FusedSort fs{c->bidx, c->bcnt, c->boff, cap};
@@ -1264,6 +1265,13 @@ int integrate_adaptive(nsg_ctx *c)
         int32_t *cid = reinterpret_cast<int32_t *>(c->lc_early + (size_t)kLcEarlyCap * 8);
         uint32_t *csrc = reinterpret_cast<uint32_t *>(c->lc_early + (size_t)kLcEarlyCap * 12);
         uint32_t *lsrc = reinterpret_cast<uint32_t *>(c->lc_early + (size_t)kLcEarlyCap * 16);
+        if (fz) {
+            // the index scatter needs nothing from the list: it runs beside the pre-pass
+            e = cudaEventRecord(c->ev_fork, s);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+            if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
+            if (int rc = bucket_fused_prepare(c, c->side)) return rc;
+        }
         {
             ProfScope ps(c, "lc_prepass", (double)c->n * 8);
             k_lc_early_collect<<<grid_for(c, c->n, 256, 4), 256, 0, s>>>(a, radius_key_host(c->p.lc_radius), ckey,
@@ -1271,8 +1279,9 @@ int integrate_adaptive(nsg_ctx *c)
             k_lc_early_rank<<<1, 1024, kLcRankSmem, s>>>(a, ckey, cid, csrc, lsrc);
             c->launches += 2;
         }
-        e = cudaEventRecord(c->ev_fork, s);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+        // the side stream's consumer reads whether the list was made (lc_early_ok)
+        e = cudaEventRecord(fz ? c->ev_pre : c->ev_fork, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, fz ? c->ev_pre : c->ev_fork, 0);
         if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
         {
             ProfScope ps(c, "levi_civita", 0.0);
@@ -1284,7 +1293,7 @@ int integrate_adaptive(nsg_ctx *c)
         if (fz) {
             // sort + level 0 in one kernel; it lists the Levi-Civita particles itself
             // when the list before the sort overflowed
-            if (int rc = fused_level0(c, a, ls, true)) return rc;
+            if (int rc = fused_level0(c, a, ls, true, true)) return rc;
         } else {
             const cudaStream_t keep = c->stream;
             c->stream = c->side;

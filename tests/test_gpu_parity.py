@@ -525,3 +525,25 @@ def test_reupload_keeps_splitters_and_results(nsg, oracle):
             want = oracle.sort(r2 * scale, v2, l2, i2)
             for g, o in zip(got, want):
                 assert np.array_equal(g, o)
+
+
+@pytest.mark.parametrize("method", [2, 5])
+def test_aux_column_follows_particles_through_fused_sorts(nsg, oracle, method):
+    """carry_aux = 1: the fifth column (mu) is permuted with the state by every sort,
+    including the sorts done inside the fused kernels; r, v_r, ell and the order equal
+    the oracle's (which has no fifth column) and mu stays attached to its particle."""
+    n = 40_000
+    r, vr, ell, ids = _adaptive_case(n, 71, lowl=100)
+    mu = np.cos(ids.astype(np.float64) * 0.001)          # a function of the id
+    kw = dict(dt=1e-3, max_subdiv=64, lc_rule=1, lc_radius=5e-2) if method == 5 else dict(dt=1e-3)
+    p = oracle.params(**kw)
+    cur = (r, vr, ell, ids) if method == 5 else oracle.sort(r, vr, ell, ids)
+    for _ in range(6):
+        cur = (oracle.step_adaptive(p, *cur)[:4] if method == 5 else oracle.step_kdk(p, *cur))
+    with _ctx(nsg, method=method, carry_aux=1, **kw) as c:
+        c.upload(r, vr, ell, ids, mu)
+        c.step(6)
+        gr, gv, gl, gid, gmu = c.download(with_aux=True)
+    assert np.array_equal(gid, cur[3]) and np.array_equal(gr, cur[0]) and np.array_equal(gv, cur[1])
+    assert np.array_equal(gl, cur[2])
+    assert np.array_equal(gmu, np.cos(gid.astype(np.float64) * 0.001))

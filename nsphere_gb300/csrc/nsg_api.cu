@@ -560,7 +560,8 @@ static int setup_segments(nsg_ctx *c, const int64_t *seg_n, int nseg)
     if (nb > c->nb_cap) {
         F(c->split); F(c->bcnt); F(c->boff);
         e = cudaMalloc((void **)&c->split, (size_t)nb * 8);
-        if (e == cudaSuccess) e = cudaMalloc((void **)&c->bcnt, (size_t)nb * 4);
+        // counts (two-kernel path: [nb]; fused path: nb look-back words and an overflow word)
+        if (e == cudaSuccess) e = cudaMalloc((void **)&c->bcnt, (size_t)nb * 8 + 8);
         if (e == cudaSuccess) e = cudaMalloc((void **)&c->boff, (size_t)nb * 4);
         if (e != cudaSuccess) return cuda_err(c, e, "bucket buffers");
         c->nb_cap = nb;

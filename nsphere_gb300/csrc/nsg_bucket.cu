@@ -97,12 +97,15 @@ k_bucket_scatter(const double *__restrict__ r, const int32_t *__restrict__ id, i
 // particle tests its home bucket with both bounding splitters read at once -- the
 // common case, a particle that did not cross a splitter -- and walks or searches
 // only when it did.  A warp whose particles all fall in one bucket appends them
-// with one atomic, in position order.
+// with one atomic, in position order.  Counts go to the low word of the bucket's
+// look-back word (cnt[2 b]); a particle past its bucket's capacity sets *over and the
+// fallback status (the consumer then hands the sort to the radix path).
 constexpr int kScatterItems = 8;
 
 __global__ void __launch_bounds__(256)
 k_bucket_scatter_idx(const double *__restrict__ r, int64_t n, const uint64_t *__restrict__ S, Seg sg, int bshift,
-                     int cap, unsigned int *__restrict__ cnt, uint32_t *__restrict__ bidx, DevCounters *ctr)
+                     int cap, unsigned int *__restrict__ cnt, unsigned int *__restrict__ over,
+                     uint32_t *__restrict__ bidx, DevCounters *ctr)
 {
     const int64_t p0 = (int64_t)blockIdx.x * (256 * kScatterItems);
     double rv[kScatterItems];
@@ -138,18 +141,23 @@ k_bucket_scatter_idx(const double *__restrict__ r, int64_t n, const uint64_t *__
         unsigned slot;
         if (__all_sync(0xffffffffu, !valid || b == b0)) {
             unsigned base = 0;
-            if (lane == 0) base = atomicAdd(&cnt[b0], (unsigned)__popc(act));
+            if (lane == 0) base = atomicAdd(&cnt[2 * b0], (unsigned)__popc(act));
             base = __shfl_sync(0xffffffffu, base, 0);
             slot = base + __popc(act & lanemask_lt());
         } else {
             const unsigned peers = __match_any_sync(0xffffffffu, b);
             const int leader = __ffs(peers) - 1;
             unsigned base = 0;
-            if (lane == leader && valid) base = atomicAdd(&cnt[b], (unsigned)__popc(peers));
+            if (lane == leader && valid) base = atomicAdd(&cnt[2 * b], (unsigned)__popc(peers));
             base = __shfl_sync(0xffffffffu, base, leader);
             slot = base + __popc(peers & lanemask_lt());
         }
-        if (valid && slot < (unsigned)cap) bidx[(int64_t)b * cap + slot] = (uint32_t)p;
+        const bool fits = slot < (unsigned)cap;
+        if (valid && fits) bidx[(int64_t)b * cap + slot] = (uint32_t)p;
+        if (__any_sync(0xffffffffu, valid && !fits) && lane == 0) {
+            *over = 1u;
+            atomicOr(&ctr->status, NSG_ST_SORT_FALLBACK);
+        }
     }
     if (nan_seen) atomicOr(&ctr->status, NSG_ST_NAN);
 }
@@ -518,26 +526,27 @@ bool use_fused(const nsg_ctx *c)
     return c->split_valid && c->p.sort_mode == 0 && fused_cap(c) > 0;
 }
 
-// Scatter and scan of the fused path: after this, bucket b's particle indices are in
-// c->bidx[b * cap ..] and its first sorted position in c->boff[b]; an overfull
-// bucket sets need_fallback (the fused kernels then return at once and the radix
-// sort with the two-kernel consumers runs instead).
+// Scatter of the fused path: after this, bucket b's particle indices are in
+// c->bidx[b * cap ..] and its count in the low word of its look-back word
+// (FusedSort); an overfull bucket sets the overflow word, and the fused kernel then
+// sets need_fallback and returns at once (the radix sort with the two-kernel
+// consumers runs instead).  The bucket starts are found inside the fused kernel.
 int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s)
 {
     const int64_t n = c->n;
     const int src = c->cur;
     const int cap = fused_cap(c);
     const int nb = (int)c->nb_total;
-    cudaError_t e = cudaMemsetAsync(c->bcnt, 0, (size_t)nb * 4, s);
+    // look-back words [nb] and the overflow word (+ pad)
+    cudaError_t e = cudaMemsetAsync(c->bcnt, 0, (size_t)nb * 8 + 8, s);
     if (e != cudaSuccess) return cuda_err(c, e, "bucket count reset");
     {
         ProfScope ps(c, "bucket_scatter", (double)n * (8 + 4), s);
         const int64_t blocks = (n + 256 * kScatterItems - 1) / (256 * kScatterItems);
         k_bucket_scatter_idx<<<(unsigned)blocks, 256, 0, s>>>(c->r[src], n, c->split, seg_table(c), c->tune.bshift,
-                                                               cap, c->bcnt, c->bidx, c->ctr);
-        k_bucket_scan<<<1, 1024, 0, s>>>(c->bcnt, nb, cap, c->boff, c->ctr);
+                                                               cap, c->bcnt, c->bcnt + 2 * nb, c->bidx, c->ctr);
     }
-    c->launches += 2;
+    c->launches += 1;
     e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "bucket scatter kernels");
 }

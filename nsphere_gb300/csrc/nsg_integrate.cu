@@ -240,19 +240,23 @@ __global__ void __launch_bounds__(512) k_gather_level0(StepArgs a)
 template <bool AUX, int T>
 __global__ void __launch_bounds__(T, T == 128 ? 6 : (T == 256 ? 4 : 1)) k_fused_level0(StepArgs a, FusedSort fs)
 {
-    if (a.ctr->need_fallback) return;
+    const unsigned over = *fs.over;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.ctr->need_fallback = over;   // read after this kernel
+    if (over) return;
     const int b = blockIdx.x;
-    const uint32_t m = fs.cnt[b];
-    if (m == 0u) return;
+    const uint32_t m = fused_count(fs, b);
+    if (m == 0u) {
+        fused_lookback_empty<T>(fs, b);
+        return;
+    }
     extern __shared__ __align__(16) unsigned char fsm[];
     uint64_t *sr, *sv;
-    fused_bucket_sort<T>(fs, b, m, a.r_src, a.id_src, fsm, sr, sv);
+    const int64_t base = fused_bucket_sort<T>(fs, b, m, a.r_src, a.id_src, fsm, sr, sv);
     const double Mpt = a.ctr->point_mass;
     const bool last = (a.nlev <= 1);
     const int h = halo_of_bucket(a.seg, b);
     const int64_t hs = a.seg.nseg <= 1 ? 0 : a.seg.start[h];
     const int64_t hn = a.seg.nseg <= 1 ? a.n : a.seg.start[h + 1] - hs;
-    const int64_t base = fs.off[b];
     for (uint32_t j = threadIdx.x; j < m; j += T) {
         const int64_t i = base + j;
         const uint64_t e = sv[j];
@@ -1196,7 +1200,7 @@ static int fused_level0(nsg_ctx *c, StepArgs &a, cudaStream_t st, bool select, b
         if (int rc = bucket_fused_prepare(c, st)) return rc;
     a.perm = a.perm_w = c->vals[0];   // the radix fallback's even pass count ends in vals[0] too
     const int cap = fused_cap(c);
-    const FusedSort fs{c->bidx, c->bcnt, c->boff, cap};
+    const FusedSort fs = fused_sort_args(c, cap);
     {
         // algorithmic bytes: index 4, r id 12, v ell 16, write r v ell id 28, inv 4, level 1
         ProfScope ps(c, "fused_level0", (double)c->n * (4 + 12 + 16 + 28 + 4 + 1 + (c->p.carry_aux ? 16 : 0)), st);

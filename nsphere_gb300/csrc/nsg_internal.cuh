@@ -113,7 +113,8 @@ struct nsg_ctx {
     // near-sorted bucket sort (nsg_bucket.cu)
     uint64_t *split = nullptr;       // [nb_total] splitter keys from the last sort
     bool split_valid = false;
-    unsigned int *bcnt = nullptr, *boff = nullptr;  // [nb]
+    unsigned int *bcnt = nullptr;    // [2 nb + 2]: counts [nb] (two-kernel path), look-back words (fused)
+    unsigned int *boff = nullptr;    // [nb] bucket starts (two-kernel path)
     uint64_t *bkey = nullptr, *bpay = nullptr;      // [nb * bucket_cap] (two-kernel path)
     int64_t bslot_cap = 0;                          // entries allocated in bkey, bpay
     uint32_t *bidx = nullptr;                       // [nb * fused_cap] (fused path)
@@ -438,7 +439,7 @@ int compute_energy(nsg_ctx *c);                       // K, W of the sorted live
 int bucket_sort_perm(nsg_ctx *c);                     // near-sorted fast path (sets need_fallback)
 int fused_cap(const nsg_ctx *c);                      // entries of a fused sort block (0: fused path off)
 int bucket_cap(const nsg_ctx *c);                     // slots per bucket of the two-kernel path
-int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s); // scatter indices + scan for the fused kernels
+int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s); // scatter indices and counts for the fused kernels
 bool use_fused(const nsg_ctx *c);                     // the sort of this step runs inside its consumer
 // Launches the radix sort and then `tail` on stream s so that they run only when
 // need_fallback is set: in a captured step as the body of a conditional graph node,

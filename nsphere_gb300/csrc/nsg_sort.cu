@@ -249,7 +249,8 @@ k_gather_rank_force(const uint32_t *__restrict__ perm, int64_t n,
 }
 
 // The same pass with the near-sorted sort done in the block (nsg_fused.cuh): block b
-// sorts bucket b and writes its sorted positions off[b] .. off[b] + cnt[b] - 1.
+// sorts bucket b and writes its sorted positions off[b] .. off[b] + cnt[b] - 1
+// (off[b] from the look-back over the counts, nsg_fused.cuh).
 template <bool AUX, bool KICK, int T>
 __global__ void __launch_bounds__(T, T == 128 ? 8 : (T == 256 ? 4 : 2))
 k_fused_rank_force(FusedSort fs, int64_t n,
@@ -259,20 +260,24 @@ k_fused_rank_force(FusedSort fs, int64_t n,
                    double *__restrict__ r1, double *__restrict__ v1, double *__restrict__ l1,
                    int32_t *__restrict__ id1, double *__restrict__ x1,
                    double *__restrict__ a0, int32_t *__restrict__ inv, uint64_t *__restrict__ split,
-                   double G, double M, double dt, const DevCounters *__restrict__ ctr, Seg sg)
+                   double G, double M, double dt, DevCounters *__restrict__ ctr, Seg sg)
 {
-    if (ctr->need_fallback) return;
+    const unsigned over = *fs.over;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr->need_fallback = over;   // read after this kernel
+    if (over) return;
     const int b = blockIdx.x;
-    const uint32_t m = fs.cnt[b];
-    if (m == 0u) return;
+    const uint32_t m = fused_count(fs, b);
+    if (m == 0u) {
+        fused_lookback_empty<T>(fs, b);
+        return;
+    }
     extern __shared__ __align__(16) unsigned char fsm[];
     uint64_t *sr, *sv;
-    fused_bucket_sort<T>(fs, b, m, r0, id0, fsm, sr, sv);
+    const int64_t base = fused_bucket_sort<T>(fs, b, m, r0, id0, fsm, sr, sv);
     const double Mpt = ctr->point_mass;
     const int h = halo_of_bucket(sg, b);
     const int64_t hs = sg.nseg <= 1 ? 0 : sg.start[h];
     const int64_t hn = sg.nseg <= 1 ? n : sg.start[h + 1] - hs;
-    const int64_t base = fs.off[b];
     for (uint32_t j = threadIdx.x; j < m; j += T) {
         const int64_t p = base + j;
         const Local L{p - hs, hn, h};
@@ -518,7 +523,7 @@ static void launch_fused_force(nsg_ctx *c, bool kick, cudaStream_t s)
     const int64_t n = c->n;
     const int src = c->cur, dst = 1 - c->cur;
     const int cap = fused_cap(c);
-    const FusedSort fs{c->bidx, c->bcnt, c->boff, cap};
+    const FusedSort fs = fused_sort_args(c, cap);
     const size_t sm = fused_smem_bytes(cap);
     const int nb = (int)c->nb_total;
 #define NSG_FUSED(AUXV, KICKV)                                                                          \

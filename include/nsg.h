@@ -62,6 +62,7 @@ extern "C" {
 #define NSG_ST_SORT_FALLBACK 0x8u /* the near-sorted bucket sort overflowed; the full radix sort ran */
 #define NSG_ST_QUEUE 0x10u        /* a work queue overflowed (internal error) */
 #define NSG_ST_IC_REJECT 0x20u    /* an initial-condition rejection loop gave up (nsg_generate) */
+#define NSG_ST_DEVICE_WAIT 0x40u  /* a bounded device wait (tensor-core completion) gave up (internal error) */
 
 /* Initial-condition models of nsg_generate. */
 #define NSG_IC_PLUMMER 1    /* Plummer sphere, Aarseth-Henon-Wielen speeds */

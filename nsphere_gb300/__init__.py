@@ -24,6 +24,7 @@ SCHED_PLAIN, SCHED_LEARNED = 0, 1
 IC_PLUMMER, IC_HERNQUIST = 1, 2
 PSI_CORED, PSI_PLUMMER, PSI_HERNQUIST = 0, 1, 2
 ST_IC_REJECT = 0x20
+ST_DEVICE_WAIT = 0x40
 ST_NAN, ST_TAU_CAP, ST_NOT_CONVERGED, ST_SORT_FALLBACK, ST_QUEUE = 0x1, 0x2, 0x4, 0x8, 0x10
 
 # exported symbols of include/nsg.h (tests check the library exports each one)

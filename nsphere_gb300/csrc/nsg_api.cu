@@ -1058,7 +1058,7 @@ int nsg_sync(nsg_ctx *c, int timeout_ms)
     }
     uint32_t st = 0;
     nsg_status(c, &st);
-    if (st & (NSG_ST_TAU_CAP | NSG_ST_QUEUE))
+    if (st & (NSG_ST_TAU_CAP | NSG_ST_QUEUE | NSG_ST_DEVICE_WAIT))
         return set_err(c, NSG_EDEVICE, "device status word 0x" + std::to_string(st));
     return NSG_OK;
 }

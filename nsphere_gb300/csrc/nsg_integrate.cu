@@ -62,7 +62,7 @@ struct StepArgs {
     double *q_r, *q_v;          // their fine N=1 result (the coarse pass of level 1)
     uint32_t *lc_idx;
     const uint32_t *lc_src;     // source index of each list entry when listed before the sort, or null
-    const int8_t *pred;         // learned schedule: predicted level per position, or null
+    const int8_t *pred;         // learned schedule: predicted level per source index, or null
     Seg seg;                    // halos of an ensemble (ranks and sizes are per halo)
     const unsigned *run_if;     // consumers of the radix fallback: return at once unless *run_if
     uint32_t *perm_w;           // fused path: source index of each Levi-Civita particle's position
@@ -187,7 +187,7 @@ __device__ __forceinline__ void level0_particle(const StepArgs &a, int64_t i, co
     const double af = acc_leap(r, gn, l2);
     // learned schedule: a particle predicted to need level >= 1 goes straight to
     // the level-parallel kernel, which tests every level from 0 upward
-    const bool fresh = (a.pred != nullptr) && !last && a.pred[i] >= 1;
+    const bool fresh = (a.pred != nullptr) && !last && a.pred[s] >= 1;
     double rc = 0.0, vc = 0.0, rf = 0.0, vf = 0.0;
     bool done = false;
     if (!fresh) {
@@ -1245,12 +1245,23 @@ int integrate_adaptive(nsg_ctx *c)
     const bool early = lc && c->p.lc_rule == NSG_LC_RADIUS;
     const bool learned = (c->p.sched == NSG_SCHED_LEARNED);
     // the sort runs inside the level-0 kernel unless something needs the permutation
-    // before it: the scheduler's features, or a Levi-Civita list made after the sort
-    const bool fz = use_fused(c) && !learned && !c->mlp_collect && (early || !lc);
+    // before it: scheduler data collection (its samples pair features with levels
+    // through it), or a Levi-Civita list made after the sort
+    const bool fz = use_fused(c) && !c->mlp_collect && (early || !lc);
     if (!early && !fz)
         if (int rc = sort_perm(c)) return rc;
     StepArgs a = make_args(c);
     const bool learned_lv = learned && a.nlev > 1;
+    // The scheduler's features come from the state as the step starts (source index
+    // order, the previous sort's); its predictions are read by source index in the
+    // level-0 pass.  Collection computes the same features.
+    auto schedule = [&](cudaStream_t st) -> int {
+        if (learned_lv)
+            if (int rc = mlp_predict_state(c, &a.pred, st)) return rc;
+        if (c->mlp_collect)
+            if (int rc = mlp_features_state(c, st)) return rc;
+        return NSG_OK;
+    };
     cudaStream_t s = c->stream;
     cudaError_t e;
     // reset queue counters (lc_count, qcount[], lc_next, lc_cand, lc_early_ok lead DevCounters)
@@ -1275,6 +1286,7 @@ int integrate_adaptive(nsg_ctx *c)
             if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
             if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
             if (int rc = bucket_fused_prepare(c, c->side)) return rc;
+            if (int rc = schedule(c->side)) return rc;
         }
         {
             ProfScope ps(c, "lc_prepass", (double)c->n * 8);
@@ -1299,6 +1311,7 @@ int integrate_adaptive(nsg_ctx *c)
             // when the list before the sort overflowed
             if (int rc = fused_level0(c, a, ls, true, true)) return rc;
         } else {
+            if (int rc = schedule(c->side)) return rc;
             const cudaStream_t keep = c->stream;
             c->stream = c->side;
             const int rc = sort_perm(c);
@@ -1317,6 +1330,7 @@ int integrate_adaptive(nsg_ctx *c)
             launch_levi_civita(c, a, s);   // the list made after the sort; empty otherwise
         }
     } else if (lc) {
+        if (int rc = schedule(s)) return rc;
         {
             ProfScope ps(c, "lc_select", (double)c->n * 20);
             k_lc_select<<<grid_for(c, c->n, 256, 4), 256, 0, s>>>(a);
@@ -1328,14 +1342,11 @@ int integrate_adaptive(nsg_ctx *c)
         ls = c->side;
         ProfScope ps(c, "levi_civita", 0.0);
         launch_levi_civita(c, a, s);
-    } else if (fz) {
-        if (int rc = fused_level0(c, a, s, false)) return rc;
+    } else {
+        if (int rc = schedule(s)) return rc;
+        if (fz)
+            if (int rc = fused_level0(c, a, s, false)) return rc;
     }
-    // the scheduler's features and predictions run beside the Levi-Civita chains too
-    if (learned_lv)
-        if (int rc = mlp_predict_sorted(c, &a.pred, ls)) return rc;
-    if (c->mlp_collect)
-        if (int rc = mlp_features_sorted(c, ls)) return rc;
     if (!fz) launch_gather_level0(c, a, ls, "gather_level0");
     if (a.nlev > 1) {
         ProfScope ps(c, "leap_levels", 0.0, ls);

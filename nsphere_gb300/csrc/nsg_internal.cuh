@@ -458,8 +458,8 @@ void track_free(nsg_ctx *c);
 int post_psi_sorted(nsg_ctx *c, const double *r, const double *v, const double *l, int64_t n, double *psi,
                     double *E, double *tile, double *total);  // Psi_A of a sorted state (nsg_post.cu)
 int64_t post_tiles(int64_t n);                           // scratch doubles post_psi_sorted needs
-int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred, cudaStream_t st);  // predicted level per sorted position
-int mlp_features_sorted(nsg_ctx *c, cudaStream_t st);  // features of the sort (training set)
+int mlp_predict_state(nsg_ctx *c, const int8_t **pred, cudaStream_t st);   // predicted level per source index
+int mlp_features_state(nsg_ctx *c, cudaStream_t st);   // features of the step's start state (training set)
 int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)
 void mlp_free(nsg_ctx *c);
 int bucket_setup(nsg_ctx *c);

@@ -1,9 +1,13 @@
 // nsg_mlp.cu -- the learned level scheduler: a 4 -> 64 -> 64 -> 8 MLP that predicts
 // the adaptive-leapfrog level a particle will accept, with BF16 weights, FP32
-// accumulation, hand-written inference and training kernels on the tensor cores
-// (mma.sync m16n8k16 bf16).
+// accumulation, hand-written inference and training kernels on the tensor cores:
+// inference (the part that runs every learned step) on the fifth-generation tensor
+// cores (tcgen05.mma with the accumulators in tensor memory, nsg_tc.cuh), 128
+// particles per MMA; training (a few small launches per epoch) with mma.sync
+// m16n8k16 warp tiles.
 //
-// Inputs per particle (FP32, computed from the sorted state at the step start):
+// Inputs per particle (FP32, computed from the state as the step starts, in its array
+// order -- the previous sort's -- whose position stands for the rank):
 //   x0 = log2(r) / 8
 //   x1 = clamp(v_r / v_c, -8, 8) / 4          v_c = sqrt(-gnum / r) = sqrt(G M_i / r)
 //   x2 = log2(|ell| / (r v_c) + 1e-6) / 8     circularity
@@ -11,15 +15,17 @@
 // Output: softmax over 8 classes, class k = accepted level k (7 also = never).
 //
 // Prediction never changes a result: in learned mode a particle predicted to need
-// level >= 1 skips the level-0 pass of k_gather_level0 and goes straight to the
-// level-parallel kernel, which still tests every level from 0 upward in the
-// reference's order (the plain error test judges every particle).
+// level >= 1 skips the level-0 pass (k_fused_level0, or k_gather_level0 on the
+// two-kernel path) and goes straight to the level-parallel kernel, which still tests
+// every level from 0 upward in the reference's order (the plain error test judges
+// every particle).
 //
 // Weight layout (float master copy and bf16 copy, row-major [out][in]):
 //   W1 [64][16] (inputs 4..15 zero), b1[64], W2 [64][64], b2[64], W3 [8][64], b3[8].
 #include <cuda_bf16.h>
 
 #include "nsg_internal.cuh"
+#include "nsg_tc.cuh"
 
 namespace nsg {
 
@@ -98,14 +104,18 @@ __device__ __forceinline__ float f32_trunc(double x)
 // r times it, log of dt over the local dynamical time r / v_c, with v_c^2 = -gn / r
 // from the rank force numerator gn (also in FP32: the features steer only which
 // level is tried first, never a result).
+// The arithmetic uses the fast hardware forms (approximate logarithm, reciprocal
+// square root and division): the features steer, so a few ulp do not matter, and
+// training and inference compute them with this same function.
 __device__ __forceinline__ void mlp_features(double r, double v, double ell, float gnf, float dtf, float f[4])
 {
     const float rf = fmaxf(f32_trunc(r), 1e-30f);
-    const float vc = sqrtf(fmaxf(-gnf / rf, 1e-30f));
-    f[0] = log2f(rf) * 0.125f;
-    f[1] = fminf(fmaxf(f32_trunc(v) / vc, -8.f), 8.f) * 0.25f;
-    f[2] = log2f(fabsf(f32_trunc(ell)) / (rf * vc) + 1e-6f) * 0.125f;
-    f[3] = log2f(dtf * vc / rf + 1e-30f) * 0.125f;
+    const float vc2 = fmaxf(__fdividef(-gnf, rf), 1e-30f);
+    const float vc = vc2 * rsqrtf(vc2);
+    f[0] = __log2f(rf) * 0.125f;
+    f[1] = fminf(fmaxf(__fdividef(f32_trunc(v), vc), -8.f), 8.f) * 0.25f;
+    f[2] = __log2f(__fdividef(fabsf(f32_trunc(ell)), rf * vc) + 1e-6f) * 0.125f;
+    f[3] = __log2f(__fdividef(dtf * vc, rf) + 1e-30f) * 0.125f;
 }
 
 // Forward pass of one 16-row tile held by a warp.  x: this thread's rows g and g+8,
@@ -223,7 +233,6 @@ __device__ __forceinline__ void tile_inputs(const float (&f)[4], int base, float
 }
 
 struct MlpStepArgs {
-    const uint32_t *perm;
     const double *r_src, *v_src, *l_src;
     int64_t n;
     double G, M, dt;
@@ -231,48 +240,265 @@ struct MlpStepArgs {
     Seg seg;
 };
 
-// Features of every sorted position (FP32), or predictions (argmax class), from the
-// sorted order given by perm.  One warp = 32 positions = two 16-row tiles.
-template <bool PREDICT>
+// The scheduler's features are those of the state as a step starts, in its array
+// order: the previous sort's, so the position of source index i within its halo
+// stands for its rank in M(r) = (rank / N) M (exact when nothing crossed since; the
+// features only steer which level is tried first).  Feature row of source index i:
+__device__ __forceinline__ void state_features(const MlpStepArgs &s, int64_t i, float Gf, float Mf, float Mptf,
+                                               float dtf, double r, double v, double ell, float (&f)[4])
+{
+    const Local L = local_of(s.seg, i, s.n);
+    const float gnf = -Gf * ((float)(int32_t)L.i / (float)(int32_t)L.n) * Mf - Gf * Mptf;
+    mlp_features(r, v, ell, gnf, dtf, f);
+}
+
+// Features of every particle by source index, kept for the training set (collect
+// mode).
 __global__ void __launch_bounds__(256) k_mlp_features(MlpStepArgs s, MlpDev m)
 {
-    __shared__ __nv_bfloat16 sW[kParams];
-    __shared__ float sB[kBias];
-    if (PREDICT) mlp_stage(m, sW, sB);
     const float Gf = f32_trunc(s.G), Mf = f32_trunc(s.M), Mptf = f32_trunc(s.ctr->point_mass);
     const float dtf = f32_trunc(s.dt);
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    for (int64_t base = gw * 32; base < s.n; base += warps * 32) {
-        const int64_t i = base + lane;
-        float f[4] = {0.f, 0.f, 0.f, 0.f};
-        if (i < s.n) {
-            const uint32_t src = s.perm[i];
-            const Local L = local_of(s.seg, i, s.n);
-            const float gnf = -Gf * ((float)(int32_t)L.i / (float)(int32_t)L.n) * Mf - Gf * Mptf;
-            mlp_features(s.r_src[src], s.v_src[src], s.l_src[src], gnf, dtf, f);
-            if (!PREDICT)
-                for (int q = 0; q < 4; q++) m.feat[i * 4 + q] = f[q];
-        }
-        if (PREDICT) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < s.n; i += (int64_t)gridDim.x * blockDim.x) {
+        float f[4];
+        state_features(s, i, Gf, Mf, Mptf, dtf, s.r_src[i], s.v_src[i], s.l_src[i], f);
+        *reinterpret_cast<float4 *>(m.feat + i * 4) = make_float4(f[0], f[1], f[2], f[3]);
+    }
+}
+
+// ------------------------------------------------------------------ inference (tcgen05)
+//
+// One CTA of 128 threads runs tiles of 128 particles; thread t owns row t of the tile
+// (tensor-memory lane t).  Per tile:
+//   X [128 x 16] (features, bf16; columns 4..15 zero)       -> shared memory
+//   D = X W1^T        (one MMA, M = 128, N = 64, K = 16)     -> tensor memory
+//   H = bf16(relu(D + b1))                                   -> shared memory
+//   D = H W2^T        (four MMAs, K = 64)                    -> tensor memory
+//   H = bf16(relu(D + b2))                                   -> shared memory
+//   D = H W3^T        (four MMAs, N = 16: W3's 8 rows and 8 zero rows)
+//   logits = D[:, 0..8) + b3, class = first argmax
+// One thread issues the MMAs and commits them to an mbarrier that the CTA waits on
+// (a bounded wait: on giving up it sets NSG_ST_DEVICE_WAIT).  The weights stay in
+// shared memory for the whole launch; the three layers reuse one 64-column
+// accumulator, read out before the next layer's MMAs are issued.
+constexpr uint32_t kTcRows = 128;                             // particles per tile (MMA M)
+constexpr uint32_t kTcN3 = 16;                                // layer-3 N
+constexpr uint32_t kTcCols = 64;                              // tensor-memory columns per CTA
+constexpr uint32_t kTcW1 = 0;                                 // W1 [64 x 16]
+constexpr uint32_t kTcW2 = kTcW1 + kH * kIn * 2;              // W2 [64 x 64]
+constexpr uint32_t kTcW3 = kTcW2 + kH * kH * 2;               // W3 [16 x 64]
+constexpr uint32_t kTcHid = kTcW3 + kTcN3 * kH * 2;           // H [128 x 64]
+// X [128 x 16] is H's first 16 columns (the same layout): it is read by the layer-1
+// MMA, which completes before H is written, and rewritten after the layer-3 MMA,
+// the last reader of H, completed
+constexpr uint32_t kTcX = kTcHid;
+constexpr uint32_t kTcBias = kTcHid + kTcRows * kH * 2;       // b1, b2, b3 (FP32)
+constexpr uint32_t kTcBar = kTcBias + kBias * 4;              // mbarrier
+constexpr uint32_t kTcSlot = kTcBar + 8;                      // tensor-memory address
+constexpr uint32_t kTcSmem = kTcSlot + 8;                      // 29 KB: seven CTAs per SM
+constexpr uint32_t kTcWaitLimit = 1u << 22;                   // mbarrier polls before giving up
+static_assert(kTcBar % 8 == 0 && kTcSlot + 8 <= kTcSmem, "mbarrier alignment, shared-memory size");
+// every byte an MMA reads lies inside its operand (last element of each operand)
+static_assert(tc_offset(kTcRows, kTcRows - 1, kIn - 1) < kTcRows * kIn * 2, "X layout");
+static_assert(tc_offset(kTcRows, kTcRows - 1, kH - 1) < kTcRows * kH * 2, "H layout");
+static_assert(tc_offset(kH, kH - 1, kIn - 1) < kH * kIn * 2, "W1 layout");
+static_assert(tc_offset(kH, kH - 1, kH - 1) < kH * kH * 2, "W2 layout");
+static_assert(tc_offset(kTcN3, kTcN3 - 1, kH - 1) < kTcN3 * kH * 2, "W3 layout");
+static_assert(3 * tc_lbo(kTcRows) * 2 + tc_lbo(kTcRows) + 15 * kTcSbo + 128 <= kTcRows * kH * 2, "last H MMA");
+
+// bf16(relu(a + b)) of two columns at once: one paired FP32 addition (IEEE round to
+// nearest, as the scalar form), one paired conversion, relu as a paired bf16 maximum
+// with zero (rounding is monotone and keeps the sign, so relu after rounding is
+// relu before it).
+__device__ __forceinline__ uint32_t bias_relu_bf16x2(float a0, float a1, float2 b)
+{
+    unsigned long long x, y = (unsigned long long)__float_as_uint(b.x) | ((unsigned long long)__float_as_uint(b.y) << 32);
+    x = (unsigned long long)__float_as_uint(a0) | ((unsigned long long)__float_as_uint(a1) << 32);
+    unsigned long long z;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(z) : "l"(x), "l"(y));
+    uint32_t p, q;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(p) : "f"(__uint_as_float((uint32_t)(z >> 32))),
+        "f"(__uint_as_float((uint32_t)z)));
+    asm("max.bf16x2 %0, %1, %2;" : "=r"(q) : "r"(p), "r"(0u));
+    return q;
+}
+
+// One hidden layer's epilogue for this thread's row: 64 accumulator columns from
+// tensor memory, + bias, relu, bf16, into row t of H.
+__device__ __forceinline__ void tc_hidden_row(uint32_t trow, const float *__restrict__ bias, unsigned char *hid, int t)
+{
+    const float4 *b4 = reinterpret_cast<const float4 *>(bias);
 #pragma unroll
-            for (int tile = 0; tile < 2; tile++) {
-                float xa[2][2];
-                tile_inputs(f, tile * 16, xa);
-                float lg[4];
-                mlp_forward_tile(sW, sB, xa, lg, nullptr, nullptr);
-                int c0, c1;
-                tile_argmax(lg, c0, c1);
-                const int g = lane >> 2;
-                if ((lane & 3) == 0) {
-                    const int64_t p0 = base + tile * 16 + g, p1 = p0 + 8;
-                    if (p0 < s.n) m.pred[p0] = (int8_t)c0;
-                    if (p1 < s.n) m.pred[p1] = (int8_t)c1;
+    for (int c = 0; c < 4; c++) {
+        float v[1][16];
+        tc_ld16(trow + 16 * c, v[0]);
+        tc_wait_ld();
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int k0 = 16 * c + 8 * h;
+            const float4 bA = b4[k0 / 4], bB = b4[k0 / 4 + 1];
+            const float *a = &v[0][8 * h];
+            const uint32_t q0 = bias_relu_bf16x2(a[0], a[1], make_float2(bA.x, bA.y));
+            const uint32_t q1 = bias_relu_bf16x2(a[2], a[3], make_float2(bA.z, bA.w));
+            const uint32_t q2 = bias_relu_bf16x2(a[4], a[5], make_float2(bB.x, bB.y));
+            const uint32_t q3 = bias_relu_bf16x2(a[6], a[7], make_float2(bB.z, bB.w));
+            *reinterpret_cast<uint4 *>(hid + tc_offset(kTcRows, t, k0)) = make_uint4(q0, q1, q2, q3);
+        }
+    }
+}
+
+// Completion of the MMAs committed to the barrier: warp 0 polls it (bounded), the
+// other warps wait at the CTA barrier that follows.
+__device__ __forceinline__ void tc_wait_mma(uint32_t bar, uint32_t &phase, bool &ok, int w)
+{
+    if (w == 0) ok &= mbar_wait_bounded(bar, phase, kTcWaitLimit);
+    __syncthreads();
+    phase ^= 1u;
+    tc_fence_after();
+}
+
+// Predicted class (and, for a feature list, the logits) of every particle.
+// FROM_STATE: the features of source index i from the state (state_features), class
+// into m.pred[i]; otherwise the features X[i][0..4), class into out[i], logits into
+// logits[i][0..8).
+template <bool FROM_STATE>
+__global__ void __launch_bounds__(kTcRows, 7)
+k_mlp_infer_tc(MlpStepArgs s, MlpDev m, const float *__restrict__ X, int64_t cnt, int8_t *__restrict__ out,
+               float *__restrict__ logits, unsigned int *status)
+{
+    extern __shared__ __align__(128) unsigned char tsm[];
+    const int t = threadIdx.x, w = t >> 5;
+    const uint32_t sb = smem_u32(tsm);
+    float *sB = reinterpret_cast<float *>(tsm + kTcBias);
+    const uint32_t bar = sb + kTcBar;
+    if (w == 0) tc_alloc(sb + kTcSlot, kTcCols);
+    // weights into the operand layout, 16 bytes (one row, 8 columns) at a time
+    const uint4 *wb = reinterpret_cast<const uint4 *>(m.wb);
+    for (int q = t; q < kH * 2; q += kTcRows) {
+        const int n = q >> 1, c = q & 1;
+        *reinterpret_cast<uint4 *>(tsm + kTcW1 + tc_offset(kH, n, 8 * c)) = wb[(kOffW1 + n * kIn + 8 * c) / 8];
+    }
+    for (int q = t; q < kH * 8; q += kTcRows) {
+        const int n = q >> 3, c = q & 7;
+        *reinterpret_cast<uint4 *>(tsm + kTcW2 + tc_offset(kH, n, 8 * c)) = wb[(kOffW2 + n * kH + 8 * c) / 8];
+    }
+    for (int q = t; q < (int)kTcN3 * 8; q += kTcRows) {
+        const int n = q >> 3, c = q & 7;
+        const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4 *>(tsm + kTcW3 + tc_offset(kTcN3, n, 8 * c)) =
+            n < kOut ? wb[(kOffW3 + n * kH + 8 * c) / 8] : z;
+    }
+    for (int k = t; k < kH; k += kTcRows) {
+        sB[kBB1 + k] = m.w[kOffB1 + k];
+        sB[kBB2 + k] = m.w[kOffB2 + k];
+    }
+    if (t < kOut) sB[kBB3 + t] = m.w[kOffB3 + t];
+    if (t == 0) mbar_init(bar, 1u);
+    tc_fence_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *reinterpret_cast<const uint32_t *>(tsm + kTcSlot);
+    const uint32_t trow = tmem + ((uint32_t)(32 * w) << 16);   // this warp's lanes, column 0
+    const uint32_t i64 = tc_idesc_bf16(kTcRows, kH), i16 = tc_idesc_bf16(kTcRows, kTcN3);
+    const uint32_t lX = tc_lbo(kTcRows), lW = tc_lbo(kH), lW3 = tc_lbo(kTcN3);
+
+    float Gf = 0.f, Mf = 0.f, Mptf = 0.f, dtf = 0.f;
+    if (FROM_STATE) {
+        Gf = f32_trunc(s.G); Mf = f32_trunc(s.M); Mptf = f32_trunc(s.ctr->point_mass); dtf = f32_trunc(s.dt);
+    }
+    const int64_t n = FROM_STATE ? s.n : cnt;
+    uint32_t phase = 0;
+    bool ok = true;
+    // The inputs of this thread's row of the next tile are loaded while the current
+    // tile's MMAs run (issued after layer 1, used at the top of the next tile).
+    const float4 *X4 = reinterpret_cast<const float4 *>(X);
+    double pr = 0.0, pv = 0.0, pl = 0.0;
+    float4 px = make_float4(0.f, 0.f, 0.f, 0.f);
+    {
+        const int64_t row0 = (int64_t)blockIdx.x * kTcRows + t;
+        if (row0 < n) {
+            if (FROM_STATE) { pr = s.r_src[row0]; pv = s.v_src[row0]; pl = s.l_src[row0]; }
+            else px = X4[row0];
+        }
+    }
+    for (int64_t tile = blockIdx.x; tile * (int64_t)kTcRows < n; tile += gridDim.x) {
+        const int64_t row = tile * (int64_t)kTcRows + t;
+        const int64_t nrow = row + (int64_t)gridDim.x * kTcRows;
+        float f[4] = {0.f, 0.f, 0.f, 0.f};
+        if (row < n) {
+            if (FROM_STATE) state_features(s, row, Gf, Mf, Mptf, dtf, pr, pv, pl, f);
+            else { f[0] = px.x; f[1] = px.y; f[2] = px.z; f[3] = px.w; }
+        }
+        *reinterpret_cast<uint4 *>(tsm + kTcX + tc_offset(kTcRows, t, 0)) =
+            make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), 0u, 0u);
+        *reinterpret_cast<uint4 *>(tsm + kTcX + tc_offset(kTcRows, t, 8)) = make_uint4(0u, 0u, 0u, 0u);
+        tc_fence_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {   // layer 1
+            tc_fence_after();
+            tc_mma_bf16(tmem, tc_smem_desc(sb + kTcX, lX, kTcSbo), tc_smem_desc(sb + kTcW1, lW, kTcSbo), i64, 0u);
+            tc_commit(bar);
+        }
+        tc_wait_mma(bar, phase, ok, w);
+        if (nrow < n) {
+            if (FROM_STATE) { pr = s.r_src[nrow]; pv = s.v_src[nrow]; pl = s.l_src[nrow]; }
+            else px = X4[nrow];
+        }
+        tc_hidden_row(trow, sB + kBB1, tsm + kTcHid, t);
+        tc_fence_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {   // layer 2
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t k = 0; k < 4; k++)
+                tc_mma_bf16(tmem, tc_smem_desc(sb + kTcHid + 2 * k * lX, lX, kTcSbo),
+                            tc_smem_desc(sb + kTcW2 + 2 * k * lW, lW, kTcSbo), i64, k);
+            tc_commit(bar);
+        }
+        tc_wait_mma(bar, phase, ok, w);
+        tc_hidden_row(trow, sB + kBB2, tsm + kTcHid, t);
+        tc_fence_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {   // layer 3
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t k = 0; k < 4; k++)
+                tc_mma_bf16(tmem, tc_smem_desc(sb + kTcHid + 2 * k * lX, lX, kTcSbo),
+                            tc_smem_desc(sb + kTcW3 + 2 * k * lW3, lW3, kTcSbo), i16, k);
+            tc_commit(bar);
+        }
+        tc_wait_mma(bar, phase, ok, w);
+        float lg[8];
+        tc_ld8(trow, lg);
+        tc_wait_ld();
+        tc_fence_before();   // the next tile's MMAs overwrite these columns after the barrier
+        int cls = 0;
+        float best = lg[0] + sB[kBB3];
+#pragma unroll
+        for (int j = 0; j < kOut; j++) {
+            lg[j] += sB[kBB3 + j];
+            if (j > 0 && lg[j] > best) { best = lg[j]; cls = j; }
+        }
+        if (row < n) {
+            if (FROM_STATE) {
+                m.pred[row] = (int8_t)cls;
+            } else {
+                out[row] = (int8_t)cls;
+                if (logits) {
+                    float4 *lo = reinterpret_cast<float4 *>(logits + row * 8);
+                    lo[0] = make_float4(lg[0], lg[1], lg[2], lg[3]);
+                    lo[1] = make_float4(lg[4], lg[5], lg[6], lg[7]);
                 }
             }
         }
     }
+    if (!ok) atomicOr(status, NSG_ST_DEVICE_WAIT);
+    __syncthreads();
+    tc_fence_after();
+    if (w == 0) tc_dealloc(tmem, kTcCols);
 }
 
 __device__ __forceinline__ uint32_t hash32(uint64_t x)
@@ -285,7 +511,8 @@ __device__ __forceinline__ uint32_t hash32(uint64_t x)
 // particle that needed level >= 1, and level-0 particles with probability keep0.
 // Levi-Civita particles are not leapfrog samples and are skipped.
 __global__ void __launch_bounds__(256)
-k_mlp_append(const int8_t *__restrict__ level, int64_t n, MlpDev m, uint32_t keep0, uint64_t salt)
+k_mlp_append(const int8_t *__restrict__ level, const uint32_t *__restrict__ perm, int64_t n, MlpDev m,
+             uint32_t keep0, uint64_t salt)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -295,7 +522,8 @@ k_mlp_append(const int8_t *__restrict__ level, int64_t n, MlpDev m, uint32_t kee
         if (cls == 0 && hash32(salt ^ (uint64_t)i) > keep0) continue;
         unsigned long long slot = atomicAdd(m.dcount, 1ull);
         if (slot >= (unsigned long long)m.dcap) continue;
-        for (int q = 0; q < 4; q++) m.dx[slot * 4 + q] = m.feat[i * 4 + q];
+        const uint32_t src = perm[i];   // level of sorted position i, features of its source index
+        for (int q = 0; q < 4; q++) m.dx[slot * 4 + q] = m.feat[(int64_t)src * 4 + q];
         m.dy[slot] = (int8_t)cls;
     }
 }
@@ -561,41 +789,6 @@ __global__ void k_mlp_refresh_bf16(MlpDev m)
         m.wb[k] = __float2bfloat16_rn(m.w[k]);
 }
 
-// Predictions for a list of feature vectors (tests and diagnostics).
-__global__ void __launch_bounds__(128) k_mlp_predict_list(MlpDev m, const float *__restrict__ X, int64_t cnt,
-                                                          int8_t *__restrict__ out, float *__restrict__ logits)
-{
-    __shared__ __nv_bfloat16 sW[kParams];
-    __shared__ float sB[kBias];
-    mlp_stage(m, sW, sB);
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    for (int64_t base = gw * 32; base < cnt; base += warps * 32) {
-        float f[4] = {0.f, 0.f, 0.f, 0.f};
-        if (base + lane < cnt)
-            for (int q = 0; q < 4; q++) f[q] = X[(base + lane) * 4 + q];
-        for (int tile = 0; tile < 2; tile++) {
-            float xa[2][2];
-            tile_inputs(f, tile * 16, xa);
-            float lg[4];
-            mlp_forward_tile(sW, sB, xa, lg, nullptr, nullptr);
-            int c0, c1;
-            tile_argmax(lg, c0, c1);
-            const int g = lane >> 2, t = lane & 3;
-            const int64_t p0 = base + tile * 16 + g, p1 = p0 + 8;
-            if (t == 0) {
-                if (p0 < cnt) out[p0] = (int8_t)c0;
-                if (p1 < cnt) out[p1] = (int8_t)c1;
-            }
-            if (logits) {
-                if (p0 < cnt) { logits[p0 * 8 + 2 * t] = lg[0]; logits[p0 * 8 + 2 * t + 1] = lg[1]; }
-                if (p1 < cnt) { logits[p1 * 8 + 2 * t] = lg[2]; logits[p1 * 8 + 2 * t + 1] = lg[3]; }
-            }
-        }
-    }
-}
-
 }  // namespace nsg
 
 namespace nsg {
@@ -629,6 +822,10 @@ static int mlp_alloc(nsg_ctx *c)
     if (e == cudaSuccess) e = cudaMemset(m->dcount, 0, sizeof(unsigned long long));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_train_smem());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_infer_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_infer_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
     c->mlp = m;
     if (e != cudaSuccess) return cuda_err(c, e, "mlp allocation");
     return NSG_OK;
@@ -662,7 +859,6 @@ static MlpStepArgs step_args(nsg_ctx *c)
 {
     MlpStepArgs s;
     const int src = c->cur;
-    s.perm = c->perm;
     s.r_src = c->r[src]; s.v_src = c->vr[src]; s.l_src = c->ell[src];
     s.n = c->n; s.G = c->p.G; s.M = c->p.M_total; s.dt = c->p.dt;
     s.ctr = c->ctr;
@@ -670,24 +866,34 @@ static MlpStepArgs step_args(nsg_ctx *c)
     return s;
 }
 
-// Predicted class per sorted position of the sort just made (c->perm, copy c->cur).
-int mlp_predict_sorted(nsg_ctx *c, const int8_t **pred, cudaStream_t st)
+// CTAs of the inference kernel: one tile of 128 particles at a time, at most seven
+// per SM (29 KB of shared memory each; 64 of the SM's 512 tensor-memory columns).
+static int infer_grid(const nsg_ctx *c, int64_t n)
+{
+    const int64_t tiles = (n + kTcRows - 1) / kTcRows;
+    const int64_t cap = (int64_t)c->num_sms * 7;
+    return (int)(tiles < cap ? (tiles > 0 ? tiles : 1) : cap);
+}
+
+// Predicted class per source index of the state as the step starts (copy c->cur).
+int mlp_predict_state(nsg_ctx *c, const int8_t **pred, cudaStream_t st)
 {
     if (!c->mlp || !c->mlp->ready) return set_err(c, NSG_ESTATE, "learned schedule needs nsg_mlp_init or trained weights");
     if (int rc = mlp_ensure_n(c)) return rc;
     ProfScope ps(c, "mlp_predict", (double)c->n * (4 + 28 + 1), st);
-    k_mlp_features<true><<<grid_for(c, c->n, 256, 4), 256, 0, st>>>(step_args(c), *c->mlp);
+    k_mlp_infer_tc<true><<<infer_grid(c, c->n), kTcRows, kTcSmem, st>>>(step_args(c), *c->mlp, nullptr, 0,
+                                                                         nullptr, nullptr, &c->ctr->status);
     c->launches += 1;
     *pred = c->mlp->pred;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "mlp predict");
 }
 
-// Features of the sort just made, kept for the training set (collect mode).
-int mlp_features_sorted(nsg_ctx *c, cudaStream_t st)
+// Features of the state as the step starts, kept for the training set (collect mode).
+int mlp_features_state(nsg_ctx *c, cudaStream_t st)
 {
     if (int rc = mlp_ensure_n(c)) return rc;
-    k_mlp_features<false><<<grid_for(c, c->n, 256, 4), 256, 0, st>>>(step_args(c), *c->mlp);
+    k_mlp_features<<<grid_for(c, c->n, 256, 4), 256, 0, st>>>(step_args(c), *c->mlp);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "mlp features");
 }
@@ -695,7 +901,7 @@ int mlp_features_sorted(nsg_ctx *c, cudaStream_t st)
 int mlp_append_levels(nsg_ctx *c)
 {
     MlpDev *m = c->mlp;
-    k_mlp_append<<<grid_for(c, c->n, 256, 4), 256, 0, c->stream>>>(c->level, c->n, *m, m->keep0,
+    k_mlp_append<<<grid_for(c, c->n, 256, 4), 256, 0, c->stream>>>(c->level, c->perm, c->n, *m, m->keep0,
                                                                   0x9E3779B97F4A7C15ull * (uint64_t)(c->steps_done + 1));
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "mlp append");
@@ -925,10 +1131,10 @@ int nsg_mlp_predict(nsg_ctx *c, const float *X, int64_t nb, int8_t *cls, float *
     if (e == cudaSuccess) e = cudaMalloc((void **)&d_l, (size_t)nb * 32);
     if (e == cudaSuccess) e = cudaMemcpy(d_X, X, (size_t)nb * 16, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        int blocks = (int)((nb + 127) / 128);
-        if (blocks > c->num_sms * 8) blocks = c->num_sms * 8;
-        k_mlp_predict_list<<<blocks, 128, 0, c->stream>>>(*c->mlp, d_X, nb, d_c, d_l);
-        e = cudaStreamSynchronize(c->stream);
+        k_mlp_infer_tc<false><<<infer_grid(c, nb), kTcRows, kTcSmem, c->stream>>>(MlpStepArgs{}, *c->mlp, d_X, nb, d_c,
+                                                                                   d_l, &c->ctr->status);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     }
     if (e == cudaSuccess) e = cudaMemcpy(cls, d_c, (size_t)nb, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && logits) e = cudaMemcpy(logits, d_l, (size_t)nb * 32, cudaMemcpyDeviceToHost);

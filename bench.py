@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--n", type=int, default=10_000_000)
     ap.add_argument("--workload", choices=["adaptive", "kdk", "ensemble", "om", "stress"], default="adaptive")
     ap.add_argument("--sched", choices=["plain", "learned"], default="plain")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--ab-steps", type=int, default=1000,
                     help="steps of each schedule in the learned/plain comparison and drift run (0: skip)")
     ap.add_argument("--train-steps", type=int, default=200, help="plain steps whose levels train the scheduler")

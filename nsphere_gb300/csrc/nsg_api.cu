@@ -883,7 +883,10 @@ int nsg_step_download(nsg_ctx *c, int nsteps, double *r, double *vr, double *ell
         if (int rc = nsg_step(c, nsteps - 1)) return rc;
     // the last step eagerly: the side stream's leapfrog kernels are followed, in stream
     // order, by the copy of the sorted state, which then runs beside the chains
-    if (int rc = one_step(c)) return rc;
+    c->gate_fallback = true;
+    const int rc1 = one_step(c);
+    c->gate_fallback = false;
+    if (rc1) return rc1;
     const int s = c->cur;
     const size_t b = (size_t)c->n * 8;
     cudaStream_t sd = c->side;

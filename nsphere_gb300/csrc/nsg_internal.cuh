@@ -69,6 +69,7 @@ struct nsg_ctx {
     cudaStream_t side = nullptr;     // leapfrog kernels beside the Levi-Civita chains
     cudaStream_t body = nullptr;     // captures the bodies of conditional graph nodes
     bool cond_nodes = false;         // the driver builds conditional graph nodes
+    bool gate_fallback = false;      // eager step of a synchronous call: read the fallback flag on the host
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_lcsel = nullptr, ev_pre = nullptr;
     bool own_stream = false;
     int device = 0;

@@ -432,6 +432,19 @@ int radix_fallback(nsg_ctx *c, cudaStream_t s, int (*tail)(nsg_ctx *, cudaStream
     int kb = 0;
     const int npass = 8 + (c->nseg > 1 ? 2 : 0);
     if (cs != cudaStreamCaptureStatusActive || !c->cond_nodes) {
+        if (cs != cudaStreamCaptureStatusActive && c->gate_fallback) {
+            // An eager step inside a call that waits for the step anyway: read whether
+            // the near-sorted path overflowed and launch the radix sort and its
+            // consumer only then (otherwise their 34-42 launches each return at once).
+            e = cudaMemcpyAsync(&c->h_ctr->need_fallback, &c->ctr->need_fallback, sizeof(unsigned),
+                                cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return cuda_err(c, e, "fallback flag");
+            if (c->h_ctr->need_fallback == 0u) {
+                c->perm = c->vals[0];   // where the near-sorted path leaves the permutation
+                return NSG_OK;
+            }
+        }
         if (int rc = launch_radix(c, s, &kb)) return rc;
         c->launches += 1 + npass * 4;
         c->perm = c->vals[kb];

@@ -79,3 +79,31 @@ def test_graph_replay_with_radix_fallback(nsg, method, cond, monkeypatch):
     assert at1.sum() == ntie and np.all(np.diff(gid[at1]) > 0)
     if method == 2:   # the fixed-step body ends with the sort; the adaptive one integrates after it
         assert np.all(np.diff(gr) >= 0)
+
+
+def test_step_download_with_radix_fallback(nsg):
+    """nsg_step_download runs its last step eagerly and reads the overflow flag on the
+    host, launching the radix sort only when the near-sorted path overflowed: with
+    10000 equal radii (no gravity) every sort overflows, and the result equals
+    nsg_step followed by nsg_download."""
+    rng = np.random.default_rng(9)
+    n, ntie = 30000, 10000
+    r = rng.uniform(0.1, 3.0, n)
+    vr = rng.normal(0.0, 0.1, n)
+    ell = rng.uniform(0.0, 0.5, n)
+    tie = rng.choice(n, ntie, replace=False)
+    r[tie], vr[tie], ell[tie] = 1.0, 0.0, 0.0
+    ids = rng.permutation(n).astype(np.int32)
+    kw = dict(dt=1e-3, G=0.0, max_subdiv=64, lc_rule=1, lc_radius=0.2, max_tau_steps=1_000_000)
+    outs = []
+    for overlapped in (False, True):
+        with nsg.Context(nsg.default_params(**kw)) as c:
+            c.upload(r, vr, ell, ids)
+            if overlapped:
+                outs.append(c.step_download(6))
+            else:
+                c.step(6)
+                outs.append(c.download())
+            assert c.status() & nsg.ST_SORT_FALLBACK
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)

@@ -547,3 +547,42 @@ def test_aux_column_follows_particles_through_fused_sorts(nsg, oracle, method):
     assert np.array_equal(gid, cur[3]) and np.array_equal(gr, cur[0]) and np.array_equal(gv, cur[1])
     assert np.array_equal(gl, cur[2])
     assert np.array_equal(gmu, np.cos(gid.astype(np.float64) * 0.001))
+
+
+@pytest.mark.parametrize("consumer", ["sort", "step"])
+def test_fused_sort_with_empty_buckets(nsg, oracle, consumer):
+    """Buckets that receive no particle: the sort's own splitters are kept across an
+    upload of a state in which every particle of buckets 0, 5 and 20 (1024 sorted
+    positions each) moved into the neighbouring buckets' key ranges.  Their blocks sort
+    nothing but still publish where the next bucket starts (the look-back over the
+    bucket counts); the fused sort (nsg_sort: rank force; nsg_step: adaptive level 0)
+    equals the oracle's with no fallback to the radix sort."""
+    n, B = 60_000, 1024
+    r, vr, ell, ids = _adaptive_case(n, 71, lowl=0)
+    kw = dict(dt=1e-3, max_subdiv=64, lc_rule=1, lc_radius=5e-2)
+    with _ctx(nsg, **kw) as c:
+        c.upload(r, vr, ell, ids)
+        c.sort()                                   # splitters: keys at positions b * 1024
+        sr, sv, sl, si = (a.copy() for a in c.download())
+        rng = np.random.default_rng(5)
+        mr = sr.copy()
+        for b in (0, 5, 20):
+            lo, hi = b * B, (b + 1) * B
+            if b == 0:                              # all into bucket 1
+                mr[lo:hi] = rng.uniform(sr[B], sr[2 * B], B)
+            else:                                   # halves into buckets b - 1 and b + 1
+                mr[lo:lo + B // 2] = rng.uniform(sr[(b - 1) * B], sr[b * B], B // 2)
+                mr[lo + B // 2:hi] = rng.uniform(sr[(b + 1) * B], sr[(b + 2) * B], B // 2)
+        c.clear_status()
+        c.upload(mr, sv, sl, si)
+        if consumer == "sort":
+            c.sort()
+            got = c.download()
+            want = oracle.sort(mr, sv, sl, si)
+        else:
+            c.step(1)
+            got = c.download()
+            want = oracle.step_adaptive(oracle.params(**kw), mr, sv, sl, si)[:4]
+        assert not c.status() & nsg.ST_SORT_FALLBACK
+    for g, o in zip(got, want):
+        assert np.array_equal(g, o)

@@ -437,6 +437,7 @@ int nsg_create(nsg_ctx **out, const nsg_params *p, void *stream)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_lcsel, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_pre, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_scat, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->body, cudaStreamNonBlocking);
     // NSG_NO_CONDITIONAL_NODES=1 takes the path of drivers without conditional nodes
     // (the radix fallback launched directly inside a captured step), for tests
@@ -479,6 +480,7 @@ void nsg_destroy(nsg_ctx *c)
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->ev_lcsel) cudaEventDestroy(c->ev_lcsel);
     if (c->ev_pre) cudaEventDestroy(c->ev_pre);
+    if (c->ev_scat) cudaEventDestroy(c->ev_scat);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->body) cudaStreamDestroy(c->body);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);

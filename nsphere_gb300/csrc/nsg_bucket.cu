@@ -27,35 +27,41 @@ constexpr int kBucketItems = 6;
 constexpr int kBucketWarps = kBucketThreads / 32;
 
 
-// Largest b in [lo, hi) with S[b] <= key (S[lo] is the smallest key of the halo),
-// searched from home.
-__device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int lo0, int hi0, uint64_t key, int home)
+// Largest b in [lo, hi) with S(b) <= key (S(lo) is the smallest key of the halo),
+// searched from home; S(b) gives splitter b.
+template <typename SplitFn>
+__device__ __forceinline__ int find_bucket_f(SplitFn S, int lo0, int hi0, uint64_t key, int home)
 {
     int b = home;
-    if (S[b] <= key) {
+    if (S(b) <= key) {
         int steps = 0;
-        while (b + 1 < hi0 && S[b + 1] <= key && steps < 8) { b++; steps++; }
-        if (b + 1 < hi0 && S[b + 1] <= key) {      // far move: binary search in (b, hi0)
-            int lo = b + 1, hi = hi0 - 1;          // S[lo] <= key
+        while (b + 1 < hi0 && S(b + 1) <= key && steps < 8) { b++; steps++; }
+        if (b + 1 < hi0 && S(b + 1) <= key) {      // far move: binary search in (b, hi0)
+            int lo = b + 1, hi = hi0 - 1;          // S(lo) <= key
             while (lo < hi) {
                 int mid = (lo + hi + 1) >> 1;
-                if (S[mid] <= key) lo = mid; else hi = mid - 1;
+                if (S(mid) <= key) lo = mid; else hi = mid - 1;
             }
             b = lo;
         }
     } else {
         int steps = 0;
-        while (b > lo0 && S[b] > key && steps < 8) { b--; steps++; }
-        if (S[b] > key) {                          // binary search in [lo0, b)
-            int lo = lo0, hi = b - 1;              // S[lo0] <= key always
+        while (b > lo0 && S(b) > key && steps < 8) { b--; steps++; }
+        if (S(b) > key) {                          // binary search in [lo0, b)
+            int lo = lo0, hi = b - 1;              // S(lo0) <= key always
             while (lo < hi) {
                 int mid = (lo + hi + 1) >> 1;
-                if (S[mid] <= key) lo = mid; else hi = mid - 1;
+                if (S(mid) <= key) lo = mid; else hi = mid - 1;
             }
             b = lo;
         }
     }
     return b;
+}
+
+__device__ __forceinline__ int find_bucket(const uint64_t *__restrict__ S, int lo0, int hi0, uint64_t key, int home)
+{
+    return find_bucket_f([S](int b) { return S[b]; }, lo0, hi0, key, home);
 }
 
 __global__ void __launch_bounds__(256)
@@ -93,71 +99,111 @@ k_bucket_scatter(const double *__restrict__ r, const int32_t *__restrict__ id, i
 }
 
 // Index scatter of the fused path, 8 particles per thread: a block takes 2048
-// consecutive positions, loads all their radii first (coalesced), then for each
-// particle tests its home bucket with both bounding splitters read at once -- the
-// common case, a particle that did not cross a splitter -- and walks or searches
-// only when it did.  A warp whose particles all fall in one bucket appends them
-// with one atomic, in position order.  Counts go to the low word of the bucket's
-// look-back word (cnt[2 b]); a particle past its bucket's capacity sets *over and the
-// fallback status (the consumer then hands the sort to the radix path).
+// consecutive positions and loads all their radii first (coalesced), and, beside
+// them, the splitters of the home buckets those positions map to (one halo:
+// position >> bshift; at most six for bucket targets of 512 and up) into shared
+// memory.  Each particle then tests its home bucket with both bounding splitters --
+// the common case, a particle that did not cross a splitter -- and walks or searches
+// only when it did.  The appends: a warp whose particles all fall in one bucket takes
+// its slots with one atomic, in position order.  Counts go to the low word of the
+// bucket's look-back word (cnt[2 b]); a particle past its bucket's capacity sets *over
+// and the fallback status (the consumer then hands the sort to the radix path).
+// COLLECT: the same pass lists the Levi-Civita candidates (radius key below lc.kthr)
+// for k_lc_early_rank, as k_lc_early_collect does.
 constexpr int kScatterItems = 8;
+constexpr int kScatterHomes = 8;                       // cached splitters [hb0, hb0 + 8)
 
-__global__ void __launch_bounds__(256)
+struct LcCollect {
+    uint64_t kthr;
+    uint64_t *ckey;
+    int32_t *cid;
+    uint32_t *csrc;
+    const int32_t *id_src;
+};
+
+template <bool COLLECT>
+__global__ void __launch_bounds__(256, 6)
 k_bucket_scatter_idx(const double *__restrict__ r, int64_t n, const uint64_t *__restrict__ S, Seg sg, int bshift,
                      int cap, unsigned int *__restrict__ cnt, unsigned int *__restrict__ over,
-                     uint32_t *__restrict__ bidx, DevCounters *ctr)
+                     uint32_t *__restrict__ bidx, DevCounters *ctr, LcCollect lc)
 {
+    __shared__ uint64_t sS[kScatterHomes];
     const int64_t p0 = (int64_t)blockIdx.x * (256 * kScatterItems);
+    const bool one = sg.nseg <= 1;
+    const int hb0 = (int)(p0 >> bshift);
     double rv[kScatterItems];
 #pragma unroll
     for (int j = 0; j < kScatterItems; j++) {
         const int64_t p = p0 + j * 256 + threadIdx.x;
         rv[j] = p < n ? r[p] : 0.0;
     }
-    bool nan_seen = false;
+    if (one && threadIdx.x < kScatterHomes) {
+        const int h = hb0 + (int)threadIdx.x;
+        sS[threadIdx.x] = h < sg.bbase[1] ? S[h] : ~0ull;   // entries past the last bucket are never read
+    }
+    __syncthreads();
+    bool nan_seen = false, overflow = false;
     const int lane = threadIdx.x & 31;
+    const int64_t wp0 = p0 + (threadIdx.x & ~31u);     // position of lane 0 at j = 0
 #pragma unroll
     for (int j = 0; j < kScatterItems; j++) {
+        if (wp0 + j * 256 >= n) break;                 // uniform: the rest of the warp's items are past the end
         const int64_t p = p0 + j * 256 + threadIdx.x;
-        if (p0 + j * 256 >= n) break;                  // the rest of the block is past the end (uniform)
-        const bool valid = p < n;
+        const bool valid = p < n;                      // a prefix of the warp's lanes, lane 0 among them
         int b = -1;
+        uint64_t key = ~0ull;
         if (valid) {
-            const double rp = rv[j];
-            const uint64_t key = radius_key(rp);
+            key = radius_key(rv[j]);
             nan_seen |= (key == ~0ull);          // NaN, tested on the integer pipe
             const Local L = local_of(sg, p, n);
             const int lo = sg.bbase[L.h], hi = sg.bbase[L.h + 1];
             int home = lo + (int)(L.i >> bshift);
             if (home >= hi) home = hi - 1;
-            const uint64_t s0 = S[home];
-            const uint64_t s1 = home + 1 < hi ? S[home + 1] : ~0ull;
+            const int q = home - hb0;
+            uint64_t s0, s1;
+            if (one && q >= 0 && q + 1 < kScatterHomes) {
+                s0 = sS[q];
+                s1 = home + 1 < hi ? sS[q + 1] : ~0ull;
+            } else {
+                s0 = S[home];
+                s1 = home + 1 < hi ? S[home + 1] : ~0ull;
+            }
             if (s0 <= key && (key < s1 || home + 1 >= hi)) b = home;
             else b = find_bucket(S, lo, hi, key, home);
         }
-        const unsigned act = __ballot_sync(0xffffffffu, valid);
-        if (act == 0u) continue;                       // lane 0 holds the warp's first position
-        const int b0 = __shfl_sync(0xffffffffu, b, 0);
-        unsigned slot;
-        if (__all_sync(0xffffffffu, !valid || b == b0)) {
-            unsigned base = 0;
-            if (lane == 0) base = atomicAdd(&cnt[2 * b0], (unsigned)__popc(act));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            slot = base + __popc(act & lanemask_lt());
-        } else {
-            const unsigned peers = __match_any_sync(0xffffffffu, b);
-            const int leader = __ffs(peers) - 1;
-            unsigned base = 0;
-            if (lane == leader && valid) base = atomicAdd(&cnt[2 * b], (unsigned)__popc(peers));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            slot = base + __popc(peers & lanemask_lt());
+        if (COLLECT) {
+            const bool cand = valid && key < lc.kthr;
+            if (__any_sync(0xffffffffu, cand)) {
+                const int slot = warp_append(cand, &ctr->lc_cand);
+                if (cand && slot < kLcEarlyCap) {
+                    lc.ckey[slot] = key;
+                    lc.cid[slot] = lc.id_src[p];
+                    lc.csrc[slot] = (uint32_t)p;
+                }
+            }
         }
+        // slots: a warp whose particles all fall in one bucket takes them with one
+        // atomic; otherwise the leader of each group of lanes with one bucket does
+        const int b0 = __shfl_sync(0xffffffffu, b, 0);
+        unsigned peers;
+        int leader = 0;
+        if (__all_sync(0xffffffffu, !valid || b == b0)) {
+            peers = __ballot_sync(0xffffffffu, valid);
+        } else {
+            peers = __match_any_sync(0xffffffffu, b);
+            leader = __ffs(peers) - 1;
+        }
+        unsigned base = 0;
+        if (lane == leader && valid) base = atomicAdd(&cnt[2 * b], (unsigned)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        const unsigned slot = base + __popc(peers & lanemask_lt());
         const bool fits = slot < (unsigned)cap;
         if (valid && fits) bidx[(int64_t)b * cap + slot] = (uint32_t)p;
-        if (__any_sync(0xffffffffu, valid && !fits) && lane == 0) {
-            *over = 1u;
-            atomicOr(&ctr->status, NSG_ST_SORT_FALLBACK);
-        }
+        overflow |= valid && !fits;
+    }
+    if (__any_sync(0xffffffffu, overflow) && lane == 0) {
+        *over = 1u;
+        atomicOr(&ctr->status, NSG_ST_SORT_FALLBACK);
     }
     if (nan_seen) atomicOr(&ctr->status, NSG_ST_NAN);
 }
@@ -531,7 +577,7 @@ bool use_fused(const nsg_ctx *c)
 // (FusedSort); an overfull bucket sets the overflow word, and the fused kernel then
 // sets need_fallback and returns at once (the radix sort with the two-kernel
 // consumers runs instead).  The bucket starts are found inside the fused kernel.
-int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s)
+int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s, uint64_t lc_thr)
 {
     const int64_t n = c->n;
     const int src = c->cur;
@@ -543,8 +589,20 @@ int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s)
     {
         ProfScope ps(c, "bucket_scatter", (double)n * (8 + 4), s);
         const int64_t blocks = (n + 256 * kScatterItems - 1) / (256 * kScatterItems);
-        k_bucket_scatter_idx<<<(unsigned)blocks, 256, 0, s>>>(c->r[src], n, c->split, seg_table(c), c->tune.bshift,
-                                                               cap, c->bcnt, c->bcnt + 2 * nb, c->bidx, c->ctr);
+        LcCollect lc{lc_thr, nullptr, nullptr, nullptr, c->id[src]};
+        if (lc_thr) {   // the early Levi-Civita list's candidate arrays (keys, ids, sources)
+            lc.ckey = reinterpret_cast<uint64_t *>(c->lc_early);
+            lc.cid = reinterpret_cast<int32_t *>(c->lc_early + (size_t)kLcEarlyCap * 8);
+            lc.csrc = reinterpret_cast<uint32_t *>(c->lc_early + (size_t)kLcEarlyCap * 12);
+        }
+        if (lc_thr)
+            k_bucket_scatter_idx<true><<<(unsigned)blocks, 256, 0, s>>>(c->r[src], n, c->split, seg_table(c),
+                                                                         c->tune.bshift, cap, c->bcnt, c->bcnt + 2 * nb,
+                                                                         c->bidx, c->ctr, lc);
+        else
+            k_bucket_scatter_idx<false><<<(unsigned)blocks, 256, 0, s>>>(c->r[src], n, c->split, seg_table(c),
+                                                                          c->tune.bshift, cap, c->bcnt, c->bcnt + 2 * nb,
+                                                                          c->bidx, c->ctr, lc);
     }
     c->launches += 1;
     e = cudaGetLastError();

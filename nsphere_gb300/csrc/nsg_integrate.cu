@@ -1280,20 +1280,26 @@ int integrate_adaptive(nsg_ctx *c)
         int32_t *cid = reinterpret_cast<int32_t *>(c->lc_early + (size_t)kLcEarlyCap * 8);
         uint32_t *csrc = reinterpret_cast<uint32_t *>(c->lc_early + (size_t)kLcEarlyCap * 12);
         uint32_t *lsrc = reinterpret_cast<uint32_t *>(c->lc_early + (size_t)kLcEarlyCap * 16);
-        if (fz) {
-            // the index scatter needs nothing from the list: it runs beside the pre-pass
-            e = cudaEventRecord(c->ev_fork, s);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
-            if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
-            if (int rc = bucket_fused_prepare(c, c->side)) return rc;
-            if (int rc = schedule(c->side)) return rc;
-        }
         {
             ProfScope ps(c, "lc_prepass", (double)c->n * 8);
-            k_lc_early_collect<<<grid_for(c, c->n, 256, 4), 256, 0, s>>>(a, radius_key_host(c->p.lc_radius), ckey,
-                                                                          cid, csrc);
+            if (fz) {
+                // one pass over the radii on the side stream: the index scatter, which
+                // also lists the candidates below lc_radius; the main stream ranks them
+                e = cudaEventRecord(c->ev_fork, s);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+                if (e != cudaSuccess) return cuda_err(c, e, "fork side stream");
+                if (int rc = bucket_fused_prepare(c, c->side, radius_key_host(c->p.lc_radius))) return rc;
+                e = cudaEventRecord(c->ev_scat, c->side);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_scat, 0);
+                if (e != cudaSuccess) return cuda_err(c, e, "scatter event");
+                if (int rc = schedule(c->side)) return rc;
+            } else {
+                k_lc_early_collect<<<grid_for(c, c->n, 256, 4), 256, 0, s>>>(a, radius_key_host(c->p.lc_radius),
+                                                                              ckey, cid, csrc);
+                c->launches += 1;
+            }
             k_lc_early_rank<<<1, 1024, kLcRankSmem, s>>>(a, ckey, cid, csrc, lsrc);
-            c->launches += 2;
+            c->launches += 1;
         }
         // the side stream's consumer reads whether the list was made (lc_early_ok)
         e = cudaEventRecord(fz ? c->ev_pre : c->ev_fork, s);

@@ -70,7 +70,7 @@ struct nsg_ctx {
     cudaStream_t body = nullptr;     // captures the bodies of conditional graph nodes
     bool cond_nodes = false;         // the driver builds conditional graph nodes
     bool gate_fallback = false;      // eager step of a synchronous call: read the fallback flag on the host
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_lcsel = nullptr, ev_pre = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_lcsel = nullptr, ev_pre = nullptr, ev_scat = nullptr;
     bool own_stream = false;
     int device = 0;
     int num_sms = 0;
@@ -440,7 +440,9 @@ int compute_energy(nsg_ctx *c);                       // K, W of the sorted live
 int bucket_sort_perm(nsg_ctx *c);                     // near-sorted fast path (sets need_fallback)
 int fused_cap(const nsg_ctx *c);                      // entries of a fused sort block (0: fused path off)
 int bucket_cap(const nsg_ctx *c);                     // slots per bucket of the two-kernel path
-int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s); // scatter indices and counts for the fused kernels
+// scatter indices and counts for the fused kernels; with lc_thr > 0 also lists the
+// Levi-Civita candidates (radius key below lc_thr) into the early-list arrays
+int bucket_fused_prepare(nsg_ctx *c, cudaStream_t s, uint64_t lc_thr = 0);
 bool use_fused(const nsg_ctx *c);                     // the sort of this step runs inside its consumer
 // Launches the radix sort and then `tail` on stream s so that they run only when
 // need_fallback is set: in a captured step as the body of a conditional graph node,

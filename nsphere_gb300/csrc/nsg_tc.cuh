@@ -14,22 +14,28 @@
 #pragma once
 #include <cstdint>
 
+#if defined(__CUDACC__)
+#define NSG_TC_HD __host__ __device__
+#else
+#define NSG_TC_HD
+#endif
+
 namespace nsg {
 
 // byte offset of element (row, k) in an R-row tile of the layout above
-__host__ __device__ constexpr uint32_t tc_offset(uint32_t R, uint32_t row, uint32_t k)
+NSG_TC_HD constexpr uint32_t tc_offset(uint32_t R, uint32_t row, uint32_t k)
 {
     return ((k / 8) * (R / 8) + row / 8) * 128 + (row % 8) * 16 + (k % 8) * 2;
 }
 
 // leading (K) and stride (row) byte offsets of an R-row tile
-__host__ __device__ constexpr uint32_t tc_lbo(uint32_t R) { return (R / 8) * 128; }
+NSG_TC_HD constexpr uint32_t tc_lbo(uint32_t R) { return (R / 8) * 128; }
 constexpr uint32_t kTcSbo = 128;
 
 // Shared-memory matrix descriptor: start address, leading and stride byte offsets
 // (all >> 4), descriptor version 1 (bits 46-47), base offset 0, layout type 0 (no
 // swizzle, bits 61-63).
-__host__ __device__ constexpr uint64_t tc_smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+NSG_TC_HD constexpr uint64_t tc_smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
 {
     return (uint64_t)((saddr >> 4) & 0x3fffu) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
            ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
@@ -38,11 +44,12 @@ __host__ __device__ constexpr uint64_t tc_smem_desc(uint32_t saddr, uint32_t lbo
 // Instruction descriptor of kind::f16: D in FP32 (bits 4-5 = 1), A and B in BF16
 // (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22,
 // M >> 4 in bits 24-28.
-__host__ __device__ constexpr uint32_t tc_idesc_bf16(uint32_t M, uint32_t N)
+NSG_TC_HD constexpr uint32_t tc_idesc_bf16(uint32_t M, uint32_t N)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
 
+#if defined(__CUDACC__)
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -144,5 +151,6 @@ __device__ __forceinline__ void tc_ld8(uint32_t taddr, float (&v)[8])
 }
 
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+#endif  // __CUDACC__
 
 }  // namespace nsg

@@ -520,7 +520,9 @@ int nsg_get_params(nsg_ctx *c, nsg_params *p)
     return NSG_OK;
 }
 
-static int validate_ids(nsg_ctx *c, const int32_t *d_id, int64_t n, unsigned int bad_in)
+// The checks of validate_ids, queued on the main stream (ids the kernels cannot
+// convert are already -1, which the count rejects).
+static int validate_ids_launch(nsg_ctx *c, const int32_t *d_id, int64_t n)
 {
     // inv doubles as the count array here
     cudaError_t e = cudaMemsetAsync(c->inv, 0, (size_t)n * 4, c->stream);
@@ -531,8 +533,16 @@ static int validate_ids(nsg_ctx *c, const int32_t *d_id, int64_t n, unsigned int
     k_check_counts<<<grid_for(c, n, 256), 256, 0, c->stream>>>(c->inv, n, d_bad);
     if (c->nseg > 1)
         k_check_halo_ids<<<grid_for(c, n, 256), 256, 0, c->stream>>>(d_id, n, seg_table(c), d_bad);
+    const cudaError_t le = cudaGetLastError();
+    return le == cudaSuccess ? NSG_OK : cuda_err(c, le, "id validation");
+}
+
+// Waits for the main stream and reports the checks' verdict.
+static int validate_ids_finish(nsg_ctx *c, unsigned int bad_in)
+{
+    unsigned int *d_bad = &c->ctr->pad;
     unsigned int bad = 0;
-    e = cudaMemcpyAsync(&c->h_ctr->pad, d_bad, 4, cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaMemcpyAsync(&c->h_ctr->pad, d_bad, 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "id validation");
     bad = c->h_ctr->pad | bad_in;
@@ -541,6 +551,12 @@ static int validate_ids(nsg_ctx *c, const int32_t *d_id, int64_t n, unsigned int
                                                   "halo's ids in its own position range"
                                                 : "particle ids must be a permutation of 0..n-1");
     return NSG_OK;
+}
+
+static int validate_ids(nsg_ctx *c, const int32_t *d_id, int64_t n, unsigned int bad_in)
+{
+    if (int rc = validate_ids_launch(c, d_id, n)) return rc;
+    return validate_ids_finish(c, bad_in);
 }
 
 // Halo table of the resident state (one halo unless an ensemble was uploaded):
@@ -657,6 +673,13 @@ static int upload_host(nsg_ctx *c, const double *r, const double *vr, const doub
         return rc;
     }
     k_ids_from_double<<<grid_for(c, n, 256), 256, 0, s>>>(c->stage_d, c->id[0], n, &c->ctr->pad);
+    // the ids are checked while the other columns are still arriving
+    if (int rc = validate_ids_launch(c, c->id[0], n)) {
+        cudaStreamSynchronize(c->side);
+        cudaStreamSynchronize(c->body);
+        cudaStreamSynchronize(s);
+        return rc;
+    }
     e = cudaEventRecord(c->ev_join, c->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_join, 0);
     if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->body);
@@ -668,7 +691,7 @@ static int upload_host(nsg_ctx *c, const double *r, const double *vr, const doub
         cudaStreamSynchronize(s);
         return rc;
     }
-    return validate_ids(c, c->id[0], n, 0);
+    return validate_ids_finish(c, 0);
 }
 
 int nsg_upload(nsg_ctx *c, const double *r, const double *vr, const double *ell,

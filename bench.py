@@ -44,9 +44,9 @@ UNIT = "particle-steps/s"
 # write them 28, write the rank force 8
 SORT_PASS_BYTES = 72.0
 # DRAM bytes per particle of one k_fused_level0 launch (read + write), from an ncu capture
-# of that kernel on the Hernquist state at N = 5e6 (176.7 MB read + 115.4 MB written per
+# of that kernel on the Hernquist state at N = 5e6 (172.8 MB read + 114.5 MB written per
 # launch; traffic grows in proportion to N)
-FUSED_LEVEL0_TRAFFIC = (176.749824e6 + 115.355136e6) / 5e6
+FUSED_LEVEL0_TRAFFIC = (172.847872e6 + 114.468352e6) / 5e6
 # DRAM bytes of one k_levi_civita_pair launch, from an ncu capture of the Hernquist step
 # at N = 2e6 (62.7 KB read, nothing written back to DRAM during the launch); it does not
 # grow with N -- the launch touches only the Levi-Civita particles

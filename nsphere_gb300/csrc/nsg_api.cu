@@ -632,6 +632,7 @@ static int upload_common(nsg_ctx *c, int64_t n, const int64_t *seg_n = nullptr, 
     const int64_t one = n;
     if (int rc = setup_segments(c, seg_n ? seg_n : &one, seg_n ? nseg : 1)) return rc;
     c->cur = 0;
+    c->state_epoch++;
     c->sorted = false;
     c->inv_valid = false;
     c->split_valid = old_split && old_start == c->h_seg_start && old_nb == c->nb_total;
@@ -821,6 +822,9 @@ static int capture_two_steps(nsg_ctx *c)
     if (e != cudaSuccess) { c->gexec = nullptr; return cuda_err(c, e, "step graph instantiate"); }
     c->g_launches = c->launches - l0;
     c->g_sorted = sorted0;
+    // the captured steps' first one took the predictions made before the capture (and
+    // its last one makes the next pair's) only when learned steps refresh them
+    c->g_pred_refresh = (c->pred_epoch == c->state_epoch);
     e = cudaGraphLaunch(c->gexec, c->stream);
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "step graph launch");
 }
@@ -840,12 +844,21 @@ int nsg_step(nsg_ctx *c, int nsteps)
             if (e != cudaSuccess) return cuda_err(c, e, "step graph launch");
             c->launches += c->g_launches;
             c->steps_done += 2;
+            c->state_epoch += 2;
+            if (c->g_pred_refresh) c->pred_epoch = c->state_epoch;
             c->p.point_mass += 2 * c->p.point_mass_rate * c->p.dt;
             if (c->p.point_mass_rate != 0.0) c->sorted = false;
             j += 2;
             continue;
         }
         if (graphable && !c->gexec) {
+            // a learned schedule's captured steps take the predictions the previous step
+            // made: make them for the current state first
+            if (c->p.sched == NSG_SCHED_LEARNED && learned_refresh(c) && c->pred_epoch != c->state_epoch) {
+                const int8_t *pred = nullptr;
+                if (int rc = mlp_predict_state(c, &pred, c->stream, c->cur)) return rc;
+                c->pred_epoch = c->state_epoch;
+            }
             if (int rc = capture_two_steps(c)) return rc;
             if (c->gexec) { j += 2; continue; }
         }

@@ -1237,6 +1237,16 @@ int fused_level0_setup(nsg_ctx *c)
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "fused level-0 attributes");
 }
 
+// Whether a learned step makes the next step's predictions at its end: one halo, the
+// fixed-radius Levi-Civita rule (whose chains own the first lc_cand rows of the new
+// order) and the fused sort.
+bool learned_refresh(const nsg_ctx *c)
+{
+    const bool lc = ((c->p.method == NSG_METHOD_ADAPTIVE_LC || c->p.method == NSG_METHOD_FULL_LC) &&
+                     c->p.lc_rule != NSG_LC_OFF);
+    return lc && c->p.lc_rule == NSG_LC_RADIUS && c->nseg <= 1 && use_fused(c) && !c->mlp_collect;
+}
+
 int integrate_adaptive(nsg_ctx *c)
 {
     const bool lc = ((c->p.method == NSG_METHOD_ADAPTIVE_LC || c->p.method == NSG_METHOD_FULL_LC) &&
@@ -1254,10 +1264,16 @@ int integrate_adaptive(nsg_ctx *c)
     const bool learned_lv = learned && a.nlev > 1;
     // The scheduler's features come from the state as the step starts (source index
     // order, the previous sort's); its predictions are read by source index in the
-    // level-0 pass.  Collection computes the same features.
+    // level-0 pass.  Collection computes the same features.  A learned step of one
+    // halo under the fixed-radius rule predicts for the next step at its own end,
+    // beside its Levi-Civita chains (whose rows, the first lc_cand of the new order,
+    // it leaves alone), so the next step starts with its predictions made.
+    const bool refresh = learned_lv && learned_refresh(c);
     auto schedule = [&](cudaStream_t st) -> int {
-        if (learned_lv)
-            if (int rc = mlp_predict_state(c, &a.pred, st)) return rc;
+        if (learned_lv) {
+            if (c->pred_epoch == c->state_epoch) a.pred = mlp_pred_buffer(c);
+            else if (int rc = mlp_predict_state(c, &a.pred, st, c->cur)) return rc;
+        }
         if (c->mlp_collect)
             if (int rc = mlp_features_state(c, st)) return rc;
         return NSG_OK;
@@ -1362,6 +1378,10 @@ int integrate_adaptive(nsg_ctx *c)
         else k_levels_lanes<false><<<c->num_sms * c->tune.lanes_bps, 256, 0, ls>>>(a, G);
         c->launches += 1;
     }
+    if (refresh) {
+        const int8_t *next = nullptr;
+        if (int rc = mlp_predict_state(c, &next, ls, 1 - c->cur, &c->ctr->lc_cand)) return rc;
+    }
     if (lc) {
         e = cudaEventRecord(c->ev_join, c->side);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_join, 0);
@@ -1372,6 +1392,8 @@ int integrate_adaptive(nsg_ctx *c)
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(c, e, "integrator kernels");
     c->cur = 1 - c->cur;
+    c->state_epoch++;
+    if (refresh) c->pred_epoch = c->state_epoch;
     c->inv_valid = true;
     c->sorted = false;  // radii moved
     c->split_valid = true;

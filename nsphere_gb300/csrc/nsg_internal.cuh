@@ -70,6 +70,10 @@ struct nsg_ctx {
     cudaStream_t body = nullptr;     // captures the bodies of conditional graph nodes
     bool cond_nodes = false;         // the driver builds conditional graph nodes
     bool gate_fallback = false;      // eager step of a synchronous call: read the fallback flag on the host
+    // the learned schedule's predictions are for the state of epoch pred_epoch; every
+    // change of the resident state (upload, sort, step) starts a new epoch
+    int64_t state_epoch = 0, pred_epoch = -1;
+    bool g_pred_refresh = false;     // the captured steps end with the next step's predictions
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_lcsel = nullptr, ev_pre = nullptr, ev_scat = nullptr;
     bool own_stream = false;
     int device = 0;
@@ -461,8 +465,12 @@ void track_free(nsg_ctx *c);
 int post_psi_sorted(nsg_ctx *c, const double *r, const double *v, const double *l, int64_t n, double *psi,
                     double *E, double *tile, double *total);  // Psi_A of a sorted state (nsg_post.cu)
 int64_t post_tiles(int64_t n);                           // scratch doubles post_psi_sorted needs
-int mlp_predict_state(nsg_ctx *c, const int8_t **pred, cudaStream_t st);   // predicted level per source index
+// predicted level per source index of the state in buffer buf (rows below *skip, when
+// given, are neither read nor predicted: class 0)
+int mlp_predict_state(nsg_ctx *c, const int8_t **pred, cudaStream_t st, int buf, const unsigned *skip = nullptr);
 int mlp_features_state(nsg_ctx *c, cudaStream_t st);   // features of the step's start state (training set)
+const int8_t *mlp_pred_buffer(nsg_ctx *c);             // the predictions' buffer (by source index)
+bool learned_refresh(const nsg_ctx *c);                // learned steps predict for the next step at their end
 int mlp_append_levels(nsg_ctx *c);                    // append (features, accepted level)
 void mlp_free(nsg_ctx *c);
 int bucket_setup(nsg_ctx *c);

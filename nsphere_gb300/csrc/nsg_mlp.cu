@@ -234,6 +234,7 @@ __device__ __forceinline__ void tile_inputs(const float (&f)[4], int base, float
 
 struct MlpStepArgs {
     const double *r_src, *v_src, *l_src;
+    const unsigned *skip;      // rows below *skip are not read (class 0); null: none
     int64_t n;
     double G, M, dt;
     const DevCounters *ctr;
@@ -407,6 +408,8 @@ k_mlp_infer_tc(MlpStepArgs s, MlpDev m, const float *__restrict__ X, int64_t cnt
         Gf = f32_trunc(s.G); Mf = f32_trunc(s.M); Mptf = f32_trunc(s.ctr->point_mass); dtf = f32_trunc(s.dt);
     }
     const int64_t n = FROM_STATE ? s.n : cnt;
+    // rows below `first` belong to the Levi-Civita chains, which may still be writing them
+    const int64_t first = (FROM_STATE && s.skip) ? (int64_t)*s.skip : 0;
     uint32_t phase = 0;
     bool ok = true;
     // The inputs of this thread's row of the next tile are loaded while the current
@@ -416,7 +419,7 @@ k_mlp_infer_tc(MlpStepArgs s, MlpDev m, const float *__restrict__ X, int64_t cnt
     float4 px = make_float4(0.f, 0.f, 0.f, 0.f);
     {
         const int64_t row0 = (int64_t)blockIdx.x * kTcRows + t;
-        if (row0 < n) {
+        if (row0 < n && row0 >= first) {
             if (FROM_STATE) { pr = s.r_src[row0]; pv = s.v_src[row0]; pl = s.l_src[row0]; }
             else px = X4[row0];
         }
@@ -425,7 +428,7 @@ k_mlp_infer_tc(MlpStepArgs s, MlpDev m, const float *__restrict__ X, int64_t cnt
         const int64_t row = tile * (int64_t)kTcRows + t;
         const int64_t nrow = row + (int64_t)gridDim.x * kTcRows;
         float f[4] = {0.f, 0.f, 0.f, 0.f};
-        if (row < n) {
+        if (row < n && row >= first) {
             if (FROM_STATE) state_features(s, row, Gf, Mf, Mptf, dtf, pr, pv, pl, f);
             else { f[0] = px.x; f[1] = px.y; f[2] = px.z; f[3] = px.w; }
         }
@@ -441,7 +444,7 @@ k_mlp_infer_tc(MlpStepArgs s, MlpDev m, const float *__restrict__ X, int64_t cnt
             tc_commit(bar);
         }
         tc_wait_mma(bar, phase, ok, w);
-        if (nrow < n) {
+        if (nrow < n && nrow >= first) {
             if (FROM_STATE) { pr = s.r_src[nrow]; pv = s.v_src[nrow]; pl = s.l_src[nrow]; }
             else px = X4[nrow];
         }
@@ -484,7 +487,7 @@ k_mlp_infer_tc(MlpStepArgs s, MlpDev m, const float *__restrict__ X, int64_t cnt
         }
         if (row < n) {
             if (FROM_STATE) {
-                m.pred[row] = (int8_t)cls;
+                m.pred[row] = row >= first ? (int8_t)cls : (int8_t)0;
             } else {
                 out[row] = (int8_t)cls;
                 if (logits) {
@@ -855,11 +858,12 @@ static int mlp_ensure_n(nsg_ctx *c)
     return NSG_OK;
 }
 
-static MlpStepArgs step_args(nsg_ctx *c)
+static MlpStepArgs step_args(nsg_ctx *c, int src = -1)
 {
     MlpStepArgs s;
-    const int src = c->cur;
+    if (src < 0) src = c->cur;
     s.r_src = c->r[src]; s.v_src = c->vr[src]; s.l_src = c->ell[src];
+    s.skip = nullptr;
     s.n = c->n; s.G = c->p.G; s.M = c->p.M_total; s.dt = c->p.dt;
     s.ctr = c->ctr;
     s.seg = seg_table(c);
@@ -876,18 +880,22 @@ static int infer_grid(const nsg_ctx *c, int64_t n)
 }
 
 // Predicted class per source index of the state as the step starts (copy c->cur).
-int mlp_predict_state(nsg_ctx *c, const int8_t **pred, cudaStream_t st)
+int mlp_predict_state(nsg_ctx *c, const int8_t **pred, cudaStream_t st, int buf, const unsigned *skip)
 {
     if (!c->mlp || !c->mlp->ready) return set_err(c, NSG_ESTATE, "learned schedule needs nsg_mlp_init or trained weights");
     if (int rc = mlp_ensure_n(c)) return rc;
     ProfScope ps(c, "mlp_predict", (double)c->n * (4 + 28 + 1), st);
-    k_mlp_infer_tc<true><<<infer_grid(c, c->n), kTcRows, kTcSmem, st>>>(step_args(c), *c->mlp, nullptr, 0,
-                                                                         nullptr, nullptr, &c->ctr->status);
+    MlpStepArgs sa = step_args(c, buf);
+    sa.skip = skip;
+    k_mlp_infer_tc<true><<<infer_grid(c, c->n), kTcRows, kTcSmem, st>>>(sa, *c->mlp, nullptr, 0, nullptr, nullptr,
+                                                                         &c->ctr->status);
     c->launches += 1;
     *pred = c->mlp->pred;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NSG_OK : cuda_err(c, e, "mlp predict");
 }
+
+const int8_t *mlp_pred_buffer(nsg_ctx *c) { return c->mlp ? c->mlp->pred : nullptr; }
 
 // Features of the state as the step starts, kept for the training set (collect mode).
 int mlp_features_state(nsg_ctx *c, cudaStream_t st)
@@ -927,6 +935,7 @@ int nsg_mlp_num_params(void) { return kParams; }
 
 int nsg_mlp_init(nsg_ctx *c, uint64_t seed)
 {
+    if (c) c->pred_epoch = -1;   // new weights: the predictions made so far are stale
     if (!c) return set_err(nullptr, NSG_EINVAL, "null context");
     mlp_quiesce(c);
     if (int rc = mlp_alloc(c)) return rc;
@@ -945,6 +954,7 @@ int nsg_mlp_init(nsg_ctx *c, uint64_t seed)
 
 int nsg_mlp_set_weights(nsg_ctx *c, const float *w, int64_t count)
 {
+    if (c) c->pred_epoch = -1;   // new weights: the predictions made so far are stale
     if (!c || !w || count != kParams) return set_err(c, NSG_EINVAL, "weights must have nsg_mlp_num_params() floats");
     mlp_quiesce(c);
     if (int rc = mlp_alloc(c)) return rc;
@@ -1066,6 +1076,7 @@ int nsg_mlp_grad(nsg_ctx *c, const float *X, const int8_t *y, int64_t nb, const 
 
 int nsg_mlp_train(nsg_ctx *c, int epochs, int batch, float lr, uint64_t seed, double *final_loss)
 {
+    if (c) c->pred_epoch = -1;   // new weights: the predictions made so far are stale
     if (!c || epochs < 0 || batch < 16 || !(lr > 0.f)) return set_err(c, NSG_EINVAL, "bad training arguments");
     if (!c->mlp || !c->mlp->ready) return set_err(c, NSG_ESTATE, "call nsg_mlp_init first");
     mlp_quiesce(c);

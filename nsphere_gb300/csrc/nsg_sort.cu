@@ -573,6 +573,7 @@ static int sort_gather(nsg_ctx *c, bool kick)
         if (int rc = launch_gather(c, kick, s, nullptr)) return rc;
     }
     c->cur = 1 - c->cur;
+    c->state_epoch++;
     c->sorted = true;
     c->inv_valid = true;
     c->split_valid = true;

@@ -78,6 +78,7 @@ int snap_put(nsg_ctx *c, const Snapshot &s)
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "tune restore");
     c->cur = k;
+    c->state_epoch++;
     c->sorted = false;
     c->inv_valid = false;
     c->split_valid = false;

@@ -47,6 +47,10 @@ SORT_PASS_BYTES = 72.0
 # of that kernel on the Hernquist state at N = 5e6 (172.8 MB read + 114.5 MB written per
 # launch; traffic grows in proportion to N)
 FUSED_LEVEL0_TRAFFIC = (172.847872e6 + 114.468352e6) / 5e6
+# DRAM bytes per particle of the fixed-step sort + scan + force pass (k_bucket_scatter_idx
+# and k_fused_rank_force with the kick), from an ncu capture of both on the Plummer state
+# at N = 5e6 (40.1 + 0.1 MB and 160.7 + 147.3 MB read + written per launch)
+SORT_PASS_TRAFFIC = (40.116224e6 + 0.082688e6 + 160.690432e6 + 147.293696e6) / 5e6
 # DRAM bytes of one k_levi_civita_pair launch, from an ncu capture of the Hernquist step
 # at N = 2e6 (62.7 KB read, nothing written back to DRAM during the launch); it does not
 # grow with N -- the launch touches only the Levi-Civita particles
@@ -596,10 +600,10 @@ def main():
             roof = dict(bulk)
         if roof is None and sort_gbs:
             # no Levi-Civita chains (fixed-step leapfrog): the sort + scan + force pass dominates
-            roof = {"bound": "hbm", "kernel": "sort + scan + force pass (k_bucket_scatter_idx, k_bucket_scan, "
-                                              "k_fused_rank_force)",
+            roof = {"bound": "hbm", "kernel": "sort + scan + force pass (k_bucket_scatter_idx, k_fused_rank_force "
+                                              "with the bucket starts by look-back)",
                     "achieved": sort_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": sort_gbs / hbm_peak,
-                    "traffic": None, "peak_source": peak_src,
+                    "traffic": SORT_PASS_TRAFFIC * n, "peak_source": peak_src,
                     "note": "72 algorithmic bytes per particle"}
         lc = by.get("levi_civita")
         line = {

@@ -349,7 +349,11 @@ int nsg_probe_latency(double *cycles, int count);
  * predicts from (r, v_r, ell, local dynamical time) the adaptive-leapfrog level each
  * particle will accept.  With params.sched = NSG_SCHED_LEARNED a particle predicted
  * to need level >= 1 skips the level-0 pass; every level is still tested from 0
- * upward, so results are bit-identical to NSG_SCHED_PLAIN. */
+ * upward, so results are bit-identical to NSG_SCHED_PLAIN.  Predictions are made on
+ * the tensor cores from the state as a step starts; a learned step of one halo under
+ * NSG_LC_RADIUS makes the next step's at its own end, beside its Levi-Civita chains.
+ * Changing the weights (init, set, train) or the state (upload, sort) makes the next
+ * step predict afresh. */
 int nsg_mlp_num_params(void);
 /* Random initial weights (seeded); allocates the network on the context. */
 int nsg_mlp_init(nsg_ctx *ctx, uint64_t seed);

@@ -451,7 +451,9 @@ def main():
 
         res_p, s_p = run_schedule(ns.SCHED_PLAIN)
         res_l, s_l = run_schedule(ns.SCHED_LEARNED)
-        same = all(np.array_equal(a_, b_) for a_, b_ in zip(s_l, s_p))
+        # bit for bit, NaN where both have NaN (the stress workload's non-finite passes)
+        same = all(np.array_equal(a_, b_, equal_nan=True) and
+                   np.array_equal(np.signbit(a_), np.signbit(b_)) for a_, b_ in zip(s_l, s_p))
         del s_l, s_p
         learned = {"train_steps": args.train_steps, "train_halo": "hernquist a=1 r<=100 isotropic, N=%d" % n,
                    "train_samples": int(len(ytrain)),

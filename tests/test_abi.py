@@ -78,3 +78,20 @@ def test_no_gpu_means_error_not_fallback(nsg):
     rc = L.nsg_create(C.byref(h), C.byref(p), None)
     assert rc == nsg.NSG_ECUDA
     assert len(L.nsg_last_error(None)) > 0
+
+
+def test_header_constants_match_python_mirror(nsg):
+    """Every NSG_* integer constant of include/nsg.h has the same value in the Python
+    mirror (status codes, status bits, methods, rules, schedules, IC models)."""
+    txt = open(os.path.join(ROOT, "include", "nsg.h")).read()
+    consts = dict(re.findall(r"#define\s+NSG_([A-Z0-9_]+)\s+\(?(-?(?:0x[0-9a-fA-F]+|\d+))u?\)?", txt))
+    assert len(consts) > 15
+    checked = 0
+    for name, val in consts.items():
+        for py in (name, "NSG_" + name):
+            if hasattr(nsg, py):
+                assert getattr(nsg, py) == int(val, 0), (name, val, getattr(nsg, py))
+                checked += 1
+                break
+    assert checked >= 15
+    assert nsg.ST_DEVICE_WAIT == 0x40
